@@ -1,0 +1,192 @@
+/* ttg.h -- C-ABI of the GB300 (sm_103a) TT-rounding library (libttgpu.so).
+ *
+ * Drop-in boundary for the reference's hot path (mva::tensor_train, a
+ * header-only C++20 library).  Each entry point names the reference
+ * interface it replaces (paths inside the reference project).  The C++20
+ * header tensor_train_gb300.hpp re-exposes the reference's own signatures on
+ * top of these functions.
+ *
+ * Data layout (identical to the reference, types/tt_core.hpp:25-212 and
+ * types/tt_matrix.hpp:29-36): a TT of order d has ranks r_0..r_d
+ * (r_0 = r_d = 1); core k is (r_k, n_k, r_{k+1}) row-major,
+ * idx = (a*n_k + i)*r_{k+1} + b.  A TT-matrix core is (r_k, m_k, n_k, r_{k+1})
+ * row-major, bit-identical to a TT core of mode m_k*n_k.  Cores are stored
+ * back to back in `data`; core k starts at data + offsets[k].
+ *
+ * Errors: every function returns a ttg_status.  The reference aborts on
+ * invalid input (fprintf + abort); the C++ header maps status != TTG_OK to
+ * exactly that, while C/ctypes callers get the code and ttg_last_error().
+ *
+ * No function here falls back to the CPU: without a usable CUDA device every
+ * compute entry point returns TTG_ERR_CUDA.
+ */
+#ifndef TTG_H
+#define TTG_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum ttg_status {
+  TTG_OK = 0,
+  TTG_ERR_ARG = 1,           /* null pointer, negative size, bad enum value */
+  TTG_ERR_SHAPE = 2,         /* rank/mode mismatch (shape_check.hpp:29-149) */
+  TTG_ERR_METHOD = 3,        /* method not valid for this entry (round.hpp:124-134) */
+  TTG_ERR_INDEX = 4,         /* eval index out of range (tt_eval.hpp:34-53) */
+  TTG_ERR_NAN = 5,           /* non-finite value met in the sweep */
+  TTG_ERR_NOT_CONVERGED = 6, /* Jacobi SVD hit its sweep limit */
+  TTG_ERR_TIMEOUT = 7,       /* a bounded device wait gave up */
+  TTG_ERR_OOM = 8,           /* device or host allocation failed */
+  TTG_ERR_CUDA = 9,          /* CUDA runtime error / no device */
+  TTG_ERR_EMPTY = 10,        /* d = 0 where the reference rejects it */
+  TTG_ERR_NO_SPACE = 11      /* a size exceeds a fixed capacity */
+} ttg_status;
+
+/* round_method (round/round.hpp:33-44).  als/dmrg are not served here. */
+typedef enum ttg_method {
+  TTG_METHOD_SVD = 0,
+  TTG_METHOD_SVD_STREAMING = 1,
+  TTG_METHOD_SVD_NAIVE = 2,
+  TTG_METHOD_ALS = 3,
+  TTG_METHOD_DMRG = 4
+} ttg_method;
+
+/* round_gauge (round/round.hpp:49-53). */
+typedef enum ttg_gauge { TTG_GAUGE_NONE = 0, TTG_GAUGE_RIGHT_CANONICAL = 1 } ttg_gauge;
+
+/* Arithmetic of the bulk contractions.  FP64 is the plain rounder. */
+typedef enum ttg_precision { TTG_PREC_FP64 = 0, TTG_PREC_MIXED = 1 } ttg_precision;
+
+/* round_options (round/round.hpp:55-105), SVD-relevant fields plus the
+ * device-side knobs.  Zero-initialise and set what you need. */
+typedef struct ttg_round_options {
+  double eps;          /* truncation tolerance (0 = exact up to rounding) */
+  int32_t max_rank;    /* 0 = unlimited */
+  int32_t method;      /* ttg_method */
+  int32_t gauge;       /* ttg_gauge */
+  int32_t precision;   /* ttg_precision */
+  int32_t max_sweeps;  /* Jacobi sweep limit, 0 = default (40) */
+  int32_t reserved;
+} ttg_round_options;
+
+/* round_result (round/round.hpp:114-119) plus per-call diagnostics. */
+typedef struct ttg_round_result {
+  int32_t iters_run;     /* 1 for the SVD path (round.hpp:196-203) */
+  int32_t converged;     /* 1 unless a Jacobi SVD hit its sweep limit */
+  double final_resid;    /* 0 for the SVD path */
+  double norm;           /* ||input|| as computed by the sweep */
+  double delta;          /* eps*||T||/sqrt(d-1) used for truncation */
+  double device_ms;      /* device time of the call's kernels */
+  int32_t status;        /* ttg_status of this tensor */
+  int32_t jacobi_sweeps; /* largest Jacobi sweep count met */
+} ttg_round_result;
+
+/* A TT (cols == NULL) or TT-matrix (rows = m_k, cols = n_k) in host memory.
+ * Inputs are read only.  Outputs written by the library own their arrays;
+ * release them with ttg_free(). */
+typedef struct ttg_tensor {
+  int32_t d;
+  int32_t* ranks;   /* d+1 */
+  int32_t* rows;    /* d: n_k (TT) or m_k (TT-matrix) */
+  int32_t* cols;    /* d: n_k of a TT-matrix; NULL for a TT */
+  int64_t* offsets; /* d+1: core k = data[offsets[k] .. offsets[k+1]) */
+  double* data;
+  int32_t owned;    /* set by the library on outputs */
+} ttg_tensor;
+
+/* ---- library ---------------------------------------------------------- */
+const char* ttg_version(void);
+const char* ttg_status_string(int32_t status);
+/* Message of the last failing call on this thread ("" if none). */
+const char* ttg_last_error(void);
+/* Number of kernel launches issued by this library since load. */
+int64_t ttg_kernel_launches(void);
+/* Releases arrays that the library allocated in *t and zeroes *t. */
+void ttg_free(ttg_tensor* t);
+
+/* ---- rounding ----------------------------------------------------------
+ * Replaces: tt round(const tt&, const round_options&, round_result*)
+ *           (round/round.hpp:230-266; engine round/tt_round.hpp:36-134 and
+ *           round_right_canonical tt_round.hpp:151-190) and the tt_matrix
+ *           overloads (round.hpp:329-425, via pack/unpack
+ *           round/tt_matrix_round.hpp:27-72) when in->cols != NULL.
+ * Rejects svd_streaming / svd_naive like round_assert_method_for_value
+ * (round.hpp:124-134); ALS/DMRG are out of scope (TTG_ERR_METHOD). */
+int32_t ttg_round(const ttg_tensor* in, const ttg_round_options* opts, ttg_tensor* out,
+                  ttg_round_result* result);
+
+/* Many independent TTs (uneven d, n, ranks) rounded in one persistent
+ * launch.  No reference counterpart takes a batch; each element follows
+ * round(const tt&, ...) (round/round.hpp:230-266).  `results` may be NULL. */
+int32_t ttg_round_batch(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
+                        ttg_tensor* outs, ttg_round_result* results);
+
+/* Replaces: void right_orthogonalize(tt&) (gauge/tt_orthogonalize.hpp:26-37)
+ * and right_orthogonalize(tt_matrix&) (gauge/tt_matrix_orthogonalize.hpp:34-86). */
+int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out);
+
+/* ---- apply + round -----------------------------------------------------
+ * Replaces: tt matvec_round(const tt_matrix&, const tt&, const round_options&,
+ *           round_result*) (round/matvec_round.hpp:42-91): svd = round(matvec)
+ *           (round/tt_matrix_apply_round.hpp:32-38), svd_streaming =
+ *           build_streaming_matvec (detail/streaming_apply.hpp:39-110). */
+int32_t ttg_matvec_round(const ttg_tensor* A, const ttg_tensor* x, const ttg_round_options* opts,
+                         ttg_tensor* out, ttg_round_result* result);
+
+/* Replaces: tt_matrix matmat_round(const tt_matrix&, const tt_matrix&, ...)
+ *           (round/matmat_round.hpp:41-93): svd = build_streaming_matmat
+ *           (detail/streaming_apply.hpp:115-202), svd_naive =
+ *           round_matrix(matmat) (round/tt_matrix_apply_round.hpp:66-72). */
+int32_t ttg_matmat_round(const ttg_tensor* A, const ttg_tensor* B, const ttg_round_options* opts,
+                         ttg_tensor* out, ttg_round_result* result);
+
+/* Replaces: tt matvec(const tt_matrix&, const tt&) and
+ *           tt_matrix matmat(const tt_matrix&, const tt_matrix&)
+ *           (apply/tt_matrix_apply.hpp:237-271): the raw rank-multiplying
+ *           products, no rounding. */
+int32_t ttg_matvec(const ttg_tensor* A, const ttg_tensor* x, ttg_tensor* out);
+int32_t ttg_matmat(const ttg_tensor* A, const ttg_tensor* B, ttg_tensor* out);
+
+/* ---- evaluation and inner products ------------------------------------
+ * Replaces: std::vector<double> eval_batch(const tt&, const int* idx, int M)
+ *           (algebra/tt_eval.hpp:86-112); idx is M x d row-major; out has M
+ *           entries (caller-owned). */
+int32_t ttg_eval_batch(const ttg_tensor* a, const int32_t* idx, int32_t M, double* out);
+
+/* Replaces: double inner(const tt&, const tt&) and double norm(const tt&)
+ *           (algebra/tt_inner.hpp:33-59). */
+int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out);
+int32_t ttg_norm(const ttg_tensor* a, double* out);
+
+/* ---- device-resident plans (inputs already in HBM) --------------------
+ * A plan owns a device arena holding a set of tensors; run() executes the
+ * sweep on `stream` (a cudaStream_t, NULL = legacy default) without host
+ * synchronisation, so it can be timed with events or captured in a graph.
+ * No reference counterpart: the reference has no device. */
+typedef struct ttg_plan ttg_plan;
+
+int32_t ttg_plan_create_round(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
+                              ttg_plan** plan);
+int32_t ttg_plan_create_matvec_round(const ttg_tensor* A, const ttg_tensor* x,
+                                     const ttg_round_options* opts, ttg_plan** plan);
+int32_t ttg_plan_create_eval(const ttg_tensor* a, const int32_t* idx, int32_t M, ttg_plan** plan);
+/* Re-uploads the inputs given at creation (host -> device) on `stream`. */
+int32_t ttg_plan_upload(ttg_plan* plan, void* stream);
+int32_t ttg_plan_run(ttg_plan* plan, void* stream);
+/* Copies results back (device -> host) and synchronises `stream`.
+ * For round plans `outs` receives `count` tensors; for eval plans
+ * `values` receives M doubles. */
+int32_t ttg_plan_download(ttg_plan* plan, void* stream, ttg_tensor* outs, double* values,
+                          ttg_round_result* results);
+/* Bytes moved host->device by upload and device->host by download. */
+int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);
+void ttg_plan_destroy(ttg_plan* plan);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TTG_H */

@@ -1,0 +1,1287 @@
+// Host runtime of libttgpu.so: the C-ABI declared in include/ttg.h.
+//
+// Validation mirrors the reference's abort conditions (types/tt.hpp:35-70,
+// detail/shape_check.hpp:29-149, round/round.hpp:124-134,
+// algebra/tt_eval.hpp:34-104) but reports them as status codes.  Every
+// compute path runs on the GPU; there is no host fallback.
+#include <algorithm>
+#include <atomic>
+#include <cmath>
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <mutex>
+#include <numeric>
+#include <string>
+#include <vector>
+
+#include <cuda_runtime.h>
+
+#include "../../include/ttg.h"
+#include "ttg_job.h"
+#include "ttg_kernels.h"
+
+using namespace ttg;
+
+namespace
+{
+
+thread_local std::string g_err;
+std::atomic<int64_t> g_launches{0};
+
+int32_t fail(int32_t st, const std::string& msg)
+{
+  g_err = msg;
+  return st;
+}
+
+#define TTG_CUDA(call)                                                               \
+  do                                                                                 \
+  {                                                                                  \
+    cudaError_t e_ = (call);                                                         \
+    if (e_ != cudaSuccess)                                                           \
+      return fail(e_ == cudaErrorMemoryAllocation ? TTG_ERR_OOM : TTG_ERR_CUDA,      \
+                  std::string(#call) + ": " + cudaGetErrorString(e_));              \
+  } while (0)
+
+struct DeviceInfo
+{
+  int ok = 0;
+  int sms = 0;
+  std::string why;
+};
+
+const DeviceInfo& device()
+{
+  static DeviceInfo info = [] {
+    DeviceInfo d;
+    int n = 0;
+    cudaError_t e = cudaGetDeviceCount(&n);
+    if (e != cudaSuccess || n == 0)
+    {
+      d.why = std::string("no CUDA device: ") + cudaGetErrorString(e);
+      return d;
+    }
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&d.sms, cudaDevAttrMultiProcessorCount, dev);
+    d.ok = 1;
+    return d;
+  }();
+  return info;
+}
+
+int32_t need_device()
+{
+  if (!device().ok)
+    return fail(TTG_ERR_CUDA, device().why);
+  return TTG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Tensor description and validation.
+// --------------------------------------------------------------------------
+struct Shape
+{
+  int d = 0;
+  bool matrix = false;
+  std::vector<int> r, m, n;  // r: d+1; m: row modes (n_k of a TT); n: col modes (1 for TT)
+  std::vector<int64_t> size, src_off;
+  const double* data = nullptr;
+  int mode(int k) const { return m[k] * n[k]; }
+};
+
+int32_t describe(const ttg_tensor* t, const char* op, Shape& s)
+{
+  if (!t)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null tensor");
+  if (t->d < 0)
+    return fail(TTG_ERR_ARG, std::string(op) + ": negative d");
+  s.d = t->d;
+  s.matrix = (t->cols != nullptr);
+  s.data = t->data;
+  if (s.d == 0)
+    return TTG_OK;
+  if (!t->ranks || !t->rows || !t->data)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null ranks/rows/data");
+  s.r.assign(t->ranks, t->ranks + s.d + 1);
+  s.m.assign(t->rows, t->rows + s.d);
+  s.n.assign(static_cast<size_t>(s.d), 1);
+  if (s.matrix)
+    s.n.assign(t->cols, t->cols + s.d);
+  for (int k = 0; k <= s.d; ++k)
+    if (s.r[k] <= 0)
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": tt_core: dimensions must be positive");
+  for (int k = 0; k < s.d; ++k)
+    if (s.m[k] <= 0 || s.n[k] <= 0)
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": tt_core: dimensions must be positive");
+  if (s.r[0] != 1)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": tt: r_0 must be 1 (got " +
+                                   std::to_string(s.r[0]) + ")");
+  if (s.r[s.d] != 1)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": tt: r_d must be 1 (got " +
+                                   std::to_string(s.r[s.d]) + ")");
+  int64_t off = 0;
+  for (int k = 0; k < s.d; ++k)
+  {
+    const int64_t sz = static_cast<int64_t>(s.r[k]) * s.mode(k) * s.r[k + 1];
+    if (sz > INT32_MAX)
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": core size exceeds INT_MAX");
+    s.size.push_back(sz);
+    const int64_t o = t->offsets ? t->offsets[k] : off;
+    if (t->offsets && t->offsets[k + 1] - t->offsets[k] != sz)
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": offsets do not match core " +
+                                     std::to_string(k) + " size");
+    s.src_off.push_back(o);
+    off += sz;
+  }
+  return TTG_OK;
+}
+
+// --------------------------------------------------------------------------
+// Device buffers.
+// --------------------------------------------------------------------------
+struct DevMem
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~DevMem() { release(); }
+  void release()
+  {
+    if (p)
+      cudaFree(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b)
+  {
+    if (b <= bytes)
+      return cudaSuccess;
+    release();
+    cudaError_t e = cudaMalloc(&p, b);
+    if (e == cudaSuccess)
+      bytes = b;
+    return e;
+  }
+};
+
+struct HostPinned
+{
+  void* p = nullptr;
+  size_t bytes = 0;
+  ~HostPinned() { release(); }
+  void release()
+  {
+    if (p)
+      cudaFreeHost(p);
+    p = nullptr;
+    bytes = 0;
+  }
+  cudaError_t ensure(size_t b)
+  {
+    if (b <= bytes)
+      return cudaSuccess;
+    release();
+    cudaError_t e = cudaHostAlloc(&p, b, cudaHostAllocDefault);
+    if (e == cudaSuccess)
+      bytes = b;
+    return e;
+  }
+};
+
+size_t align256(size_t b) { return (b + 255) & ~static_cast<size_t>(255); }
+
+// --------------------------------------------------------------------------
+// Round plan: arena + tables + scratch in one device allocation; the
+// uploaded prefix [arena | slots | tts | order | idx tables] mirrors a
+// pinned host image so upload/download are single copies.
+// --------------------------------------------------------------------------
+enum PlanKind
+{
+  kPlanRound,
+  kPlanMatvecNaive,
+  kPlanStream,
+  kPlanEval
+};
+
+}  // namespace
+
+struct ttg_plan
+{
+  PlanKind kind = kPlanRound;
+  int job_kind = kJobRound;
+  ttg_round_options opts{};
+  std::vector<Shape> shapes;       // input tensors, in arena order
+  std::vector<int> out_tts;        // TT indices returned to the caller
+  std::vector<CoreSlot> slots;
+  std::vector<TTInfo> tts;
+  std::vector<int32_t> order, a_idx, b_idx, out_idx;
+  int64_t arena_doubles = 0;
+  int64_t scratch_stride = 0;
+  int grid = 1;
+  // products computed on the device before the sweep (naive apply-round):
+  struct Apply
+  {
+    int a_slot, x_slot, y_slot, r, m, p, rp, s, nout, sp;
+  };
+  std::vector<Apply> applies;
+  // byte layout of the device buffer
+  size_t off_arena = 0, off_slots = 0, off_tts = 0, off_order = 0, off_aidx = 0, off_bidx = 0,
+         off_oidx = 0, prefix_bytes = 0, off_queue = 0, off_scratch = 0, total_bytes = 0;
+  DevMem dev;
+  HostPinned host;
+  // eval plans
+  const int32_t* eval_idx = nullptr;
+  int64_t M = 0;
+  int rcap = 0;
+  size_t off_idx = 0, off_out = 0, off_bad = 0;
+  int64_t h2d = 0, d2h = 0;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  ~ttg_plan()
+  {
+    if (ev0)
+      cudaEventDestroy(ev0);
+    if (ev1)
+      cudaEventDestroy(ev1);
+  }
+};
+
+namespace
+{
+
+int add_tensor(ttg_plan& P, const Shape& s, bool upload, const std::vector<int64_t>* cap_sizes)
+{
+  TTInfo t{};
+  t.first = static_cast<int32_t>(P.slots.size());
+  t.d = s.d;
+  for (int k = 0; k < s.d; ++k)
+  {
+    CoreSlot c{};
+    c.off = P.arena_doubles;
+    c.n = s.mode(k);
+    c.r = s.r[k];
+    c.rp = s.r[k + 1];
+    c.m = s.matrix ? s.m[k] : 0;
+    const int64_t cap = cap_sizes ? (*cap_sizes)[k] : s.size[k];
+    P.arena_doubles += a32(cap);
+    P.slots.push_back(c);
+  }
+  (void)upload;
+  P.tts.push_back(t);
+  return static_cast<int>(P.tts.size()) - 1;
+}
+
+// Scratch need of a round-type sweep over a TT with the given input dims.
+int64_t round_need(const Shape& s, int job_kind)
+{
+  int64_t need = 0;
+  const int d = s.d;
+  if (d <= 1)
+    return 64;
+  int64_t cols = 0;
+  for (int k = 0; k < d; ++k)
+  {
+    const int64_t r = s.r[k], n = s.mode(k), rp = s.r[k + 1];
+    const int64_t hp = k > 0 ? static_cast<int64_t>(s.r[k - 1]) * s.mode(k - 1) : 0;
+    const int64_t wn = k + 1 < d ? static_cast<int64_t>(s.mode(k + 1)) * s.r[k + 2] : 0;
+    if (job_kind == kJobRound || job_kind == kJobRightOrth)
+    {
+      if (k >= 1)
+        need = std::max(need, need_right_qr(r, n * rp, hp));
+      if (k <= d - 2 && job_kind == kJobRound)
+        need = std::max(need, need_svd_step(r * n, rp, wn));
+    }
+    else
+    {
+      if (k <= d - 2)
+        need = std::max(need, need_left_qr(r * n, rp, wn));
+      if (k >= 1)
+        need = std::max(need, need_svd_step_right(n * rp, r, hp));
+    }
+    if (k <= d - 2)
+      cols += rp;
+  }
+  need = std::max(need, a32(cols + 1));
+  return need + 64;
+}
+
+int64_t stream_need(const Shape& A, const Shape& X)
+{
+  const int d = A.d;
+  int64_t need = std::max(round_need(A, kJobRightOrth), round_need(X, kJobRightOrth));
+  int64_t fcap = 1;
+  for (int k = 0; k < d; ++k)
+  {
+    const int64_t cap = static_cast<int64_t>(A.r[k + 1]) * X.r[k + 1];
+    fcap = std::max(fcap, cap * cap);
+  }
+  for (int k = 0; k < d; ++k)
+  {
+    const int64_t alpha = static_cast<int64_t>(A.r[k]) * X.r[k];
+    need = std::max(need, need_stream_step(fcap, alpha, A.r[k], A.m[k], A.n[k], A.r[k + 1],
+                                           X.r[k], X.mode(k) / A.n[k], X.r[k + 1]));
+  }
+  return need + 64;
+}
+
+double est_cost(const Shape& s)
+{
+  double c = 0.0;
+  for (int k = 0; k < s.d; ++k)
+    c += static_cast<double>(s.size[k]) * std::max(s.r[k], s.r[k + 1]);
+  return c;
+}
+
+int32_t layout_and_alloc(ttg_plan& P)
+{
+  size_t o = 0;
+  P.off_arena = o;
+  o = align256(o + sizeof(double) * static_cast<size_t>(P.arena_doubles));
+  P.off_slots = o;
+  o = align256(o + sizeof(CoreSlot) * P.slots.size());
+  P.off_tts = o;
+  o = align256(o + sizeof(TTInfo) * P.tts.size());
+  P.off_order = o;
+  o = align256(o + sizeof(int32_t) * P.order.size());
+  P.off_aidx = o;
+  o = align256(o + sizeof(int32_t) * P.a_idx.size());
+  P.off_bidx = o;
+  o = align256(o + sizeof(int32_t) * P.b_idx.size());
+  P.off_oidx = o;
+  o = align256(o + sizeof(int32_t) * P.out_idx.size());
+  P.prefix_bytes = o;
+  P.off_queue = o;
+  o = align256(o + 256);
+  P.off_scratch = o;
+  o = align256(o + sizeof(double) * static_cast<size_t>(P.scratch_stride) * P.grid);
+  P.total_bytes = o;
+  TTG_CUDA(P.dev.ensure(P.total_bytes));
+  TTG_CUDA(P.host.ensure(P.prefix_bytes));
+  TTG_CUDA(cudaEventCreate(&P.ev0));
+  TTG_CUDA(cudaEventCreate(&P.ev1));
+  // Host image of the prefix: arena inputs + tables.
+  char* h = static_cast<char*>(P.host.p);
+  std::memset(h, 0, P.prefix_bytes);
+  double* arena = reinterpret_cast<double*>(h + P.off_arena);
+  for (size_t t = 0; t < P.shapes.size(); ++t)
+  {
+    const Shape& s = P.shapes[t];
+    const TTInfo& ti = P.tts[t];
+    for (int k = 0; k < s.d; ++k)
+      std::memcpy(arena + P.slots[ti.first + k].off, s.data + s.src_off[k],
+                  sizeof(double) * static_cast<size_t>(s.size[k]));
+  }
+  std::memcpy(h + P.off_slots, P.slots.data(), sizeof(CoreSlot) * P.slots.size());
+  std::memcpy(h + P.off_tts, P.tts.data(), sizeof(TTInfo) * P.tts.size());
+  std::memcpy(h + P.off_order, P.order.data(), sizeof(int32_t) * P.order.size());
+  if (!P.a_idx.empty())
+  {
+    std::memcpy(h + P.off_aidx, P.a_idx.data(), sizeof(int32_t) * P.a_idx.size());
+    std::memcpy(h + P.off_bidx, P.b_idx.data(), sizeof(int32_t) * P.b_idx.size());
+    std::memcpy(h + P.off_oidx, P.out_idx.data(), sizeof(int32_t) * P.out_idx.size());
+  }
+  P.h2d = static_cast<int64_t>(P.prefix_bytes);
+  P.d2h = static_cast<int64_t>(P.off_order);
+  return TTG_OK;
+}
+
+RoundJob make_job(ttg_plan& P)
+{
+  char* d = static_cast<char*>(P.dev.p);
+  RoundJob j{};
+  j.arena = reinterpret_cast<double*>(d + P.off_arena);
+  j.slots = reinterpret_cast<CoreSlot*>(d + P.off_slots);
+  j.tts = reinterpret_cast<TTInfo*>(d + P.off_tts);
+  j.order = reinterpret_cast<const int32_t*>(d + P.off_order);
+  j.ntt = static_cast<int32_t>(P.order.size());
+  j.kind = P.job_kind;
+  j.scratch = reinterpret_cast<double*>(d + P.off_scratch);
+  j.scratch_stride = P.scratch_stride;
+  j.queue = reinterpret_cast<int32_t*>(d + P.off_queue);
+  j.eps = P.opts.eps;
+  j.max_rank = P.opts.max_rank;
+  j.max_sweeps = P.opts.max_sweeps > 0 ? P.opts.max_sweeps : 40;
+  j.a_idx = reinterpret_cast<const int32_t*>(d + P.off_aidx);
+  j.b_idx = reinterpret_cast<const int32_t*>(d + P.off_bidx);
+  j.out_idx = reinterpret_cast<const int32_t*>(d + P.off_oidx);
+  return j;
+}
+
+int32_t check_opts(const ttg_round_options* o, const char* op)
+{
+  if (!o)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null options");
+  if (std::isnan(o->eps) || o->eps < 0.0)
+    return fail(TTG_ERR_ARG, std::string(op) + ": eps must be >= 0");
+  if (o->max_rank < 0)
+    return fail(TTG_ERR_ARG, std::string(op) + ": max_rank must be >= 0");
+  if (o->gauge != TTG_GAUGE_NONE && o->gauge != TTG_GAUGE_RIGHT_CANONICAL)
+    return fail(TTG_ERR_ARG, std::string(op) + ": unknown gauge");
+  if (o->precision != TTG_PREC_FP64)
+    return fail(TTG_ERR_METHOD, std::string(op) + ": only precision FP64 is served by this build");
+  if (o->method == TTG_METHOD_ALS || o->method == TTG_METHOD_DMRG)
+    return fail(TTG_ERR_METHOD, std::string(op) + ": als/dmrg rounding is not served here");
+  if (o->method < 0 || o->method > TTG_METHOD_DMRG)
+    return fail(TTG_ERR_METHOD, std::string(op) + ": unknown method " + std::to_string(o->method));
+  return TTG_OK;
+}
+
+int finish_grid(int64_t items)
+{
+  const int sms = std::max(device().sms, 1);
+  return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(items, 2LL * sms)));
+}
+
+int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
+                         const ttg_round_options* opts, const char* op)
+{
+  if (int32_t st = check_opts(opts, op))
+    return st;
+  if (opts->method != TTG_METHOD_SVD)
+    return fail(TTG_ERR_METHOD, std::string(op) +
+                                    ": round_method::svd_streaming / svd_naive are only valid on "
+                                    "matvec_round / matmat_round respectively.");
+  P.opts = *opts;
+  P.kind = kPlanRound;
+  P.job_kind = opts->gauge == TTG_GAUGE_RIGHT_CANONICAL ? kJobRoundRight : kJobRound;
+  P.shapes.resize(static_cast<size_t>(count));
+  int64_t need = 64;
+  std::vector<std::pair<double, int>> cost;
+  for (int i = 0; i < count; ++i)
+  {
+    if (int32_t st = describe(&ins[i], op, P.shapes[i]))
+      return st;
+    add_tensor(P, P.shapes[i], true, nullptr);
+    need = std::max(need, round_need(P.shapes[i], P.job_kind));
+    P.out_tts.push_back(i);
+    if (P.shapes[i].d > 1)
+      cost.emplace_back(est_cost(P.shapes[i]), i);
+  }
+  std::stable_sort(cost.begin(), cost.end(),
+                   [](const auto& a, const auto& b) { return a.first > b.first; });
+  for (auto& c : cost)
+    P.order.push_back(c.second);
+  P.scratch_stride = need;
+  P.grid = finish_grid(static_cast<int64_t>(P.order.size()));
+  return layout_and_alloc(P);
+}
+
+int32_t plan_upload(ttg_plan& P, cudaStream_t st)
+{
+  TTG_CUDA(cudaMemcpyAsync(P.dev.p, P.host.p, P.prefix_bytes, cudaMemcpyHostToDevice, st));
+  return TTG_OK;
+}
+
+int32_t plan_run(ttg_plan& P, cudaStream_t st)
+{
+  char* d = static_cast<char*>(P.dev.p);
+  if (P.kind == kPlanEval)
+  {
+    TTG_CUDA(cudaMemsetAsync(d + P.off_bad, 0, sizeof(int), st));
+    const Shape& s = P.shapes[0];
+    const int sms = std::max(device().sms, 1);
+    const int64_t warps_needed = (P.M + 7) / 8;
+    const int grid = static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(warps_needed, 8LL * sms)));
+    launch_eval(reinterpret_cast<double*>(d + P.off_arena),
+                reinterpret_cast<CoreSlot*>(d + P.off_slots), s.d,
+                reinterpret_cast<const int*>(d + P.off_idx), P.M,
+                reinterpret_cast<double*>(d + P.off_out), P.rcap,
+                reinterpret_cast<int*>(d + P.off_bad), grid, st);
+    g_launches += 1;
+    TTG_CUDA(cudaGetLastError());
+    return TTG_OK;
+  }
+  double* arena = reinterpret_cast<double*>(d + P.off_arena);
+  for (const auto& a : P.applies)
+  {
+    launch_apply_core(arena + P.slots[a.a_slot].off, arena + P.slots[a.x_slot].off,
+                      arena + P.slots[a.y_slot].off, a.r, a.m, a.p, a.rp, a.s, a.nout, a.sp, st);
+    g_launches += 1;
+  }
+  if (!P.order.empty() && P.job_kind >= 0)
+  {
+    TTG_CUDA(cudaMemsetAsync(d + P.off_queue, 0, sizeof(int32_t), st));
+    launch_round(make_job(P), P.grid, st);
+    g_launches += 1;
+  }
+  TTG_CUDA(cudaGetLastError());
+  return TTG_OK;
+}
+
+int32_t plan_download_raw(ttg_plan& P, cudaStream_t st)
+{
+  TTG_CUDA(cudaMemcpyAsync(P.host.p, P.dev.p, P.off_order, cudaMemcpyDeviceToHost, st));
+  TTG_CUDA(cudaStreamSynchronize(st));
+  return TTG_OK;
+}
+
+// Builds an output tensor from TT `t` of the downloaded host image.
+int32_t emit_tensor(ttg_plan& P, int t, bool matrix, const std::vector<int>& mrow,
+                    const std::vector<int>& ncol, ttg_tensor* out)
+{
+  const char* h = static_cast<const char*>(P.host.p);
+  const CoreSlot* S = reinterpret_cast<const CoreSlot*>(h + P.off_slots);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  const double* arena = reinterpret_cast<const double*>(h + P.off_arena);
+  const TTInfo& ti = T[t];
+  const int d = ti.d;
+  std::memset(out, 0, sizeof(*out));
+  out->d = d;
+  out->owned = 1;
+  out->ranks = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * (d + 1)));
+  out->rows = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max(d, 1)));
+  out->offsets = static_cast<int64_t*>(std::malloc(sizeof(int64_t) * (d + 1)));
+  if (matrix)
+    out->cols = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max(d, 1)));
+  if (!out->ranks || !out->rows || !out->offsets || (matrix && !out->cols))
+    return fail(TTG_ERR_OOM, "host allocation failed");
+  int64_t total = 0;
+  out->ranks[0] = d > 0 ? S[ti.first].r : 1;
+  for (int k = 0; k < d; ++k)
+  {
+    const CoreSlot& c = S[ti.first + k];
+    out->ranks[k + 1] = c.rp;
+    out->rows[k] = matrix ? mrow[k] : c.n;
+    if (matrix)
+      out->cols[k] = ncol[k];
+    out->offsets[k] = total;
+    total += static_cast<int64_t>(c.r) * c.n * c.rp;
+  }
+  out->offsets[d] = total;
+  out->data = static_cast<double*>(std::malloc(sizeof(double) * std::max<int64_t>(total, 1)));
+  if (!out->data)
+    return fail(TTG_ERR_OOM, "host allocation failed");
+  for (int k = 0; k < d; ++k)
+  {
+    const CoreSlot& c = S[ti.first + k];
+    std::memcpy(out->data + out->offsets[k], arena + c.off,
+                sizeof(double) * static_cast<size_t>(static_cast<int64_t>(c.r) * c.n * c.rp));
+  }
+  return TTG_OK;
+}
+
+void fill_result(const TTInfo& ti, float ms, ttg_round_result* r)
+{
+  if (!r)
+    return;
+  r->iters_run = 1;
+  r->final_resid = 0.0;
+  r->converged = ti.status == TTG_ERR_NOT_CONVERGED ? 0 : 1;
+  r->norm = ti.norm;
+  r->delta = ti.delta;
+  r->device_ms = ms;
+  r->status = ti.status;
+  r->jacobi_sweeps = ti.sweeps;
+}
+
+int32_t first_bad_status(const ttg_plan& P)
+{
+  const char* h = static_cast<const char*>(P.host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  for (size_t i = 0; i < P.tts.size(); ++i)
+    if (T[i].status != TTG_OK && T[i].status != TTG_ERR_NOT_CONVERGED)
+      return T[i].status;
+  return TTG_OK;
+}
+
+cudaStream_t lib_stream()
+{
+  static cudaStream_t s = [] {
+    cudaStream_t x = nullptr;
+    cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
+    return x;
+  }();
+  return s;
+}
+
+std::mutex g_mu;
+
+// Runs a plan end to end on the library stream with device timing.
+int32_t execute(ttg_plan& P, float* ms)
+{
+  cudaStream_t st = lib_stream();
+  if (int32_t e = plan_upload(P, st))
+    return e;
+  TTG_CUDA(cudaEventRecord(P.ev0, st));
+  if (int32_t e = plan_run(P, st))
+    return e;
+  TTG_CUDA(cudaEventRecord(P.ev1, st));
+  if (int32_t e = plan_download_raw(P, st))
+    return e;
+  TTG_CUDA(cudaEventElapsedTime(ms, P.ev0, P.ev1));
+  return TTG_OK;
+}
+
+int32_t copy_through(const Shape& s, ttg_tensor* out)
+{
+  // d <= 1: round returns its input unchanged (round/tt_round.hpp:38-42).
+  std::memset(out, 0, sizeof(*out));
+  out->d = s.d;
+  out->owned = 1;
+  out->ranks = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * (s.d + 1)));
+  out->rows = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max(s.d, 1)));
+  out->offsets = static_cast<int64_t*>(std::malloc(sizeof(int64_t) * (s.d + 1)));
+  if (s.matrix)
+    out->cols = static_cast<int32_t*>(std::malloc(sizeof(int32_t) * std::max(s.d, 1)));
+  out->ranks[0] = 1;
+  int64_t total = 0;
+  for (int k = 0; k < s.d; ++k)
+  {
+    out->ranks[k + 1] = s.r[k + 1];
+    out->rows[k] = s.m[k];
+    if (s.matrix)
+      out->cols[k] = s.n[k];
+    out->offsets[k] = total;
+    total += s.size[k];
+  }
+  out->offsets[s.d] = total;
+  out->data = static_cast<double*>(std::malloc(sizeof(double) * std::max<int64_t>(total, 1)));
+  for (int k = 0; k < s.d; ++k)
+    std::memcpy(out->data + out->offsets[k], s.data + s.src_off[k],
+                sizeof(double) * static_cast<size_t>(s.size[k]));
+  return TTG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* ttg_version(void) { return "ttgpu 0.1 (sm_103a, fp64 sweep)"; }
+
+const char* ttg_status_string(int32_t s)
+{
+  switch (s)
+  {
+    case TTG_OK: return "ok";
+    case TTG_ERR_ARG: return "invalid argument";
+    case TTG_ERR_SHAPE: return "shape mismatch";
+    case TTG_ERR_METHOD: return "method not valid here";
+    case TTG_ERR_INDEX: return "index out of range";
+    case TTG_ERR_NAN: return "non-finite value";
+    case TTG_ERR_NOT_CONVERGED: return "Jacobi SVD did not converge";
+    case TTG_ERR_TIMEOUT: return "device wait timed out";
+    case TTG_ERR_OOM: return "out of memory";
+    case TTG_ERR_CUDA: return "CUDA error";
+    case TTG_ERR_EMPTY: return "empty tensor (d = 0)";
+    case TTG_ERR_NO_SPACE: return "size exceeds a fixed capacity";
+    default: return "unknown status";
+  }
+}
+
+const char* ttg_last_error(void) { return g_err.c_str(); }
+
+int64_t ttg_kernel_launches(void) { return g_launches.load(); }
+
+void ttg_free(ttg_tensor* t)
+{
+  if (!t || !t->owned)
+    return;
+  std::free(t->ranks);
+  std::free(t->rows);
+  std::free(t->cols);
+  std::free(t->offsets);
+  std::free(t->data);
+  std::memset(t, 0, sizeof(*t));
+}
+
+int32_t ttg_plan_create_round(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
+                              ttg_plan** plan)
+{
+  g_err.clear();
+  if (!plan || count < 0 || (count > 0 && !ins))
+    return fail(TTG_ERR_ARG, "ttg_plan_create_round: bad arguments");
+  if (int32_t st = need_device())
+    return st;
+  auto* P = new ttg_plan;
+  const int32_t st = build_round_plan(*P, count, ins, opts, "round");
+  if (st)
+  {
+    delete P;
+    return st;
+  }
+  *plan = P;
+  return TTG_OK;
+}
+
+static int32_t eval_upload(ttg_plan& P, cudaStream_t st);
+
+int32_t ttg_plan_upload(ttg_plan* P, void* stream)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  if (P->kind == kPlanEval)
+    return eval_upload(*P, static_cast<cudaStream_t>(stream));
+  return plan_upload(*P, static_cast<cudaStream_t>(stream));
+}
+
+int32_t ttg_plan_run(ttg_plan* P, void* stream)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  return plan_run(*P, static_cast<cudaStream_t>(stream));
+}
+
+int32_t ttg_plan_io_bytes(const ttg_plan* P, int64_t* h2d, int64_t* d2h)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  if (h2d)
+    *h2d = P->h2d;
+  if (d2h)
+    *d2h = P->d2h;
+  return TTG_OK;
+}
+
+void ttg_plan_destroy(ttg_plan* P) { delete P; }
+
+int32_t ttg_plan_download(ttg_plan* P, void* stream, ttg_tensor* outs, double* values,
+                          ttg_round_result* results)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  if (P->kind == kPlanEval)
+  {
+    char* d = static_cast<char*>(P->dev.p);
+    int bad = 0;
+    TTG_CUDA(cudaMemcpyAsync(values, d + P->off_out, sizeof(double) * P->M,
+                             cudaMemcpyDeviceToHost, st));
+    TTG_CUDA(cudaMemcpyAsync(&bad, d + P->off_bad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    TTG_CUDA(cudaStreamSynchronize(st));
+    if (bad)
+      return fail(TTG_ERR_INDEX, "eval_at: idx out of range");
+    return TTG_OK;
+  }
+  if (int32_t e = plan_download_raw(*P, st))
+    return e;
+  const char* h = static_cast<const char*>(P->host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P->off_tts);
+  for (size_t i = 0; i < P->out_tts.size(); ++i)
+  {
+    const int t = P->out_tts[i];
+    const Shape& s = P->shapes[P->kind == kPlanRound ? t : 0];
+    bool matrix = s.matrix;
+    std::vector<int> mrow = s.m, ncol = s.n;
+    if (P->kind != kPlanRound)
+    {
+      // apply-round: rows from the operator, cols from the operand.
+      matrix = P->shapes[1].matrix;
+      mrow = P->shapes[0].m;
+      ncol = P->shapes[1].n;
+    }
+    if (outs)
+      if (int32_t e = emit_tensor(*P, t, matrix, mrow, ncol, &outs[i]))
+        return e;
+    fill_result(T[t], 0.0f, results ? &results[i] : nullptr);
+  }
+  return first_bad_status(*P) ? fail(first_bad_status(*P), "sweep reported a device status")
+                              : TTG_OK;
+}
+
+static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
+                            ttg_tensor* outs, ttg_round_result* results, const char* op)
+{
+  g_err.clear();
+  if (count < 0 || (count > 0 && (!ins || !outs)))
+    return fail(TTG_ERR_ARG, std::string(op) + ": bad arguments");
+  if (int32_t st = check_opts(opts, op))
+    return st;
+  if (opts->method != TTG_METHOD_SVD)
+    return fail(TTG_ERR_METHOD, std::string(op) +
+                                    ": round_method::svd_streaming / svd_naive are only valid on "
+                                    "matvec_round / matmat_round respectively.");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_plan P;
+  if (int32_t st = build_round_plan(P, count, ins, opts, op))
+    return st;
+  float ms = 0.0f;
+  if (int32_t st = execute(P, &ms))
+    return st;
+  const char* h = static_cast<const char*>(P.host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  for (int i = 0; i < count; ++i)
+  {
+    const Shape& s = P.shapes[i];
+    if (s.d <= 1)
+    {
+      copy_through(s, &outs[i]);
+      if (results)
+      {
+        std::memset(&results[i], 0, sizeof(results[i]));
+        results[i].iters_run = 1;
+        results[i].converged = 1;
+      }
+      continue;
+    }
+    if (int32_t e = emit_tensor(P, i, s.matrix, s.m, s.n, &outs[i]))
+      return e;
+    fill_result(T[i], ms, results ? &results[i] : nullptr);
+  }
+  if (int32_t bad = first_bad_status(P))
+    return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
+  return TTG_OK;
+}
+
+int32_t ttg_round(const ttg_tensor* in, const ttg_round_options* opts, ttg_tensor* out,
+                  ttg_round_result* result)
+{
+  return round_common(1, in, opts, out, result, "round");
+}
+
+int32_t ttg_round_batch(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
+                        ttg_tensor* outs, ttg_round_result* results)
+{
+  return round_common(count, ins, opts, outs, results, "round_batch");
+}
+
+int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
+{
+  g_err.clear();
+  if (!in || !out)
+    return fail(TTG_ERR_ARG, "right_orthogonalize: null argument");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_round_options o{};
+  ttg_plan P;
+  if (int32_t st = build_round_plan(P, 1, in, &o, "right_orthogonalize"))
+    return st;
+  P.job_kind = kJobRightOrth;
+  if (P.shapes[0].d <= 1)
+    return copy_through(P.shapes[0], out);
+  float ms = 0.0f;
+  if (int32_t st = execute(P, &ms))
+    return st;
+  return emit_tensor(P, 0, P.shapes[0].matrix, P.shapes[0].m, P.shapes[0].n, out);
+}
+
+// ---------------------------------------------------------------------------
+// Apply and apply-round.
+// ---------------------------------------------------------------------------
+static int32_t check_apply(const Shape& A, const Shape& X, bool matmat, const char* op)
+{
+  if (!A.matrix)
+    return fail(TTG_ERR_ARG, std::string(op) + ": operator must be a TT-matrix");
+  if (matmat != X.matrix)
+    return fail(TTG_ERR_ARG, std::string(op) + ": operand kind mismatch");
+  if (A.d != X.d)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": d mismatch (a.d=" + std::to_string(A.d) +
+                                   ", x.d=" + std::to_string(X.d) + ")");
+  for (int k = 0; k < A.d; ++k)
+    if (A.n[k] != X.m[k])
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": mode-size mismatch at axis " +
+                                     std::to_string(k));
+  return TTG_OK;
+}
+
+// Plan with A, X uploaded and the product TT computed by apply kernels;
+// when `round` the product is then rounded (gauge none).
+static int32_t build_apply_plan(ttg_plan& P, const Shape& A, const Shape& X, bool round,
+                                const ttg_round_options* opts)
+{
+  P.kind = kPlanMatvecNaive;
+  if (opts)
+    P.opts = *opts;
+  P.shapes = {A, X};
+  add_tensor(P, A, true, nullptr);
+  add_tensor(P, X, true, nullptr);
+  const int d = A.d;
+  const int nout_all = 1;
+  (void)nout_all;
+  Shape Y;
+  Y.d = d;
+  Y.matrix = X.matrix;
+  Y.r.resize(d + 1);
+  for (int k = 0; k <= d; ++k)
+    Y.r[k] = A.r[k] * X.r[k];
+  for (int k = 0; k < d; ++k)
+  {
+    Y.m.push_back(A.m[k]);
+    Y.n.push_back(X.n[k]);
+    Y.size.push_back(static_cast<int64_t>(Y.r[k]) * Y.mode(k) * Y.r[k + 1]);
+    Y.src_off.push_back(0);
+  }
+  const int y = add_tensor(P, Y, false, nullptr);
+  for (int k = 0; k < d; ++k)
+  {
+    ttg_plan::Apply ap{};
+    ap.a_slot = P.tts[0].first + k;
+    ap.x_slot = P.tts[1].first + k;
+    ap.y_slot = P.tts[y].first + k;
+    ap.r = A.r[k];
+    ap.m = A.m[k];
+    ap.p = A.n[k];
+    ap.rp = A.r[k + 1];
+    ap.s = X.r[k];
+    ap.nout = X.n[k];
+    ap.sp = X.r[k + 1];
+    P.applies.push_back(ap);
+  }
+  P.out_tts = {y};
+  P.job_kind = round ? kJobRound : -1;
+  if (round && d > 1)
+  {
+    P.order = {y};
+    P.scratch_stride = round_need(Y, kJobRound);
+  }
+  else
+  {
+    P.scratch_stride = 64;
+  }
+  P.grid = 1;
+  // The product shape has no host data; layout_and_alloc copies only A, X.
+  Shape* keep = &P.shapes[0];
+  (void)keep;
+  return TTG_OK;
+}
+
+static int32_t build_stream_plan(ttg_plan& P, const Shape& A, const Shape& X,
+                                 const ttg_round_options* opts)
+{
+  P.kind = kPlanStream;
+  P.opts = *opts;
+  P.shapes = {A, X};
+  add_tensor(P, A, true, nullptr);
+  add_tensor(P, X, true, nullptr);
+  const int d = A.d;
+  Shape Y;
+  Y.d = d;
+  Y.matrix = X.matrix;
+  Y.r.resize(d + 1);
+  for (int k = 0; k <= d; ++k)
+    Y.r[k] = A.r[k] * X.r[k];
+  std::vector<int64_t> caps;
+  for (int k = 0; k < d; ++k)
+  {
+    Y.m.push_back(A.m[k]);
+    Y.n.push_back(X.n[k]);
+    Y.size.push_back(static_cast<int64_t>(Y.r[k]) * Y.mode(k) * Y.r[k + 1]);
+    Y.src_off.push_back(0);
+  }
+  const int y = add_tensor(P, Y, false, nullptr);
+  P.out_tts = {y};
+  P.job_kind = X.matrix ? kJobStreamMatmat : kJobStreamMatvec;
+  P.order = {0};
+  P.a_idx = {0};
+  P.b_idx = {1};
+  P.out_idx = {y};
+  P.scratch_stride = stream_need(A, X);
+  P.grid = 1;
+  return TTG_OK;
+}
+
+static int32_t apply_round_common(const ttg_tensor* a, const ttg_tensor* x,
+                                  const ttg_round_options* opts, ttg_tensor* out,
+                                  ttg_round_result* result, bool matmat, int mode, const char* op)
+{
+  // mode: 0 = raw apply, 1 = apply then round (naive), 2 = streaming.
+  g_err.clear();
+  if (!out)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null output");
+  Shape A, X;
+  if (int32_t st = describe(a, op, A))
+    return st;
+  if (int32_t st = describe(x, op, X))
+    return st;
+  if (A.d != X.d)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": core count mismatch " + std::to_string(A.d) +
+                                   " vs " + std::to_string(X.d));
+  if (A.d > 0)
+    if (int32_t st = check_apply(A, X, matmat, op))
+      return st;
+  if (int32_t st = need_device())
+    return st;
+  if (A.d == 0)
+  {
+    std::memset(out, 0, sizeof(*out));
+    out->owned = 1;
+    out->ranks = static_cast<int32_t*>(std::malloc(sizeof(int32_t)));
+    out->offsets = static_cast<int64_t*>(std::malloc(sizeof(int64_t)));
+    out->ranks[0] = 1;
+    out->offsets[0] = 0;
+    if (result)
+    {
+      std::memset(result, 0, sizeof(*result));
+      result->iters_run = 1;
+      result->converged = 1;
+    }
+    return TTG_OK;
+  }
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_plan P;
+  int32_t st = (mode == 2) ? build_stream_plan(P, A, X, opts)
+                           : build_apply_plan(P, A, X, mode == 1, opts);
+  if (st)
+    return st;
+  // Only A and X carry host data: trim the shapes list for the upload.
+  std::vector<Shape> all = P.shapes;
+  if ((st = layout_and_alloc(P)))
+    return st;
+  float ms = 0.0f;
+  if ((st = execute(P, &ms)))
+    return st;
+  const int y = P.out_tts[0];
+  if ((st = emit_tensor(P, y, X.matrix, A.m, X.n, out)))
+    return st;
+  const char* h = static_cast<const char*>(P.host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  fill_result(T[y], ms, result);
+  if (int32_t bad = first_bad_status(P))
+    return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
+  return TTG_OK;
+}
+
+int32_t ttg_matvec_round(const ttg_tensor* A, const ttg_tensor* x, const ttg_round_options* opts,
+                         ttg_tensor* out, ttg_round_result* result)
+{
+  g_err.clear();
+  if (int32_t st = check_opts(opts, "matvec_round"))
+    return st;
+  if (opts->method == TTG_METHOD_SVD_NAIVE)
+    return fail(TTG_ERR_METHOD, "matvec_round: round_method::svd_naive is matmat-only");
+  if (opts->gauge != TTG_GAUGE_NONE)
+    return fail(TTG_ERR_ARG, "matvec_round: gauge is a round() option");
+  const bool streaming = opts->method == TTG_METHOD_SVD_STREAMING && A && A->d > 1;
+  return apply_round_common(A, x, opts, out, result, false, streaming ? 2 : 1, "matvec_round");
+}
+
+int32_t ttg_matmat_round(const ttg_tensor* A, const ttg_tensor* B, const ttg_round_options* opts,
+                         ttg_tensor* out, ttg_round_result* result)
+{
+  g_err.clear();
+  if (int32_t st = check_opts(opts, "matmat_round"))
+    return st;
+  if (opts->method == TTG_METHOD_SVD_STREAMING)
+    return fail(TTG_ERR_METHOD, "matmat_round: round_method::svd_streaming is matvec-only");
+  if (opts->gauge != TTG_GAUGE_NONE)
+    return fail(TTG_ERR_ARG, "matmat_round: gauge is a round() option");
+  const bool streaming = opts->method == TTG_METHOD_SVD && A && A->d > 1;
+  return apply_round_common(A, B, opts, out, result, true, streaming ? 2 : 1, "matmat_round");
+}
+
+int32_t ttg_matvec(const ttg_tensor* A, const ttg_tensor* x, ttg_tensor* out)
+{
+  return apply_round_common(A, x, nullptr, out, nullptr, false, 0, "matvec");
+}
+
+int32_t ttg_matmat(const ttg_tensor* A, const ttg_tensor* B, ttg_tensor* out)
+{
+  return apply_round_common(A, B, nullptr, out, nullptr, true, 0, "matmat");
+}
+
+int32_t ttg_plan_create_matvec_round(const ttg_tensor* a, const ttg_tensor* x,
+                                     const ttg_round_options* opts, ttg_plan** plan)
+{
+  g_err.clear();
+  if (!plan)
+    return fail(TTG_ERR_ARG, "null plan");
+  if (int32_t st = check_opts(opts, "matvec_round"))
+    return st;
+  if (opts->method == TTG_METHOD_SVD_NAIVE)
+    return fail(TTG_ERR_METHOD, "matvec_round: round_method::svd_naive is matmat-only");
+  if (int32_t st = need_device())
+    return st;
+  Shape A, X;
+  if (int32_t st = describe(a, "matvec_round", A))
+    return st;
+  if (int32_t st = describe(x, "matvec_round", X))
+    return st;
+  if (A.d < 2)
+    return fail(TTG_ERR_SHAPE, "plan: matvec_round plans need d >= 2");
+  if (int32_t st = check_apply(A, X, false, "matvec_round"))
+    return st;
+  auto* P = new ttg_plan;
+  int32_t st = (opts->method == TTG_METHOD_SVD_STREAMING) ? build_stream_plan(*P, A, X, opts)
+                                                          : build_apply_plan(*P, A, X, true, opts);
+  if (!st)
+    st = layout_and_alloc(*P);
+  if (st)
+  {
+    delete P;
+    return st;
+  }
+  *plan = P;
+  return TTG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// eval_batch, inner, norm.
+// ---------------------------------------------------------------------------
+static int32_t build_eval_plan(ttg_plan& P, const ttg_tensor* a, const int32_t* idx, int32_t M)
+{
+  Shape s;
+  if (int32_t st = describe(a, "eval_batch", s))
+    return st;
+  if (s.matrix)
+    return fail(TTG_ERR_ARG, "eval_batch: expects a TT");
+  if (!idx && M > 0)
+    return fail(TTG_ERR_ARG, "eval_batch: idx pointer is null with M=" + std::to_string(M) +
+                                 " > 0");
+  if (M < 0)
+    return fail(TTG_ERR_ARG, "eval_batch: M must be non-negative (got " + std::to_string(M) + ")");
+  if (s.d == 0)
+    return fail(TTG_ERR_EMPTY, "eval_batch: TT is empty (d=0)");
+  P.kind = kPlanEval;
+  P.shapes = {s};
+  add_tensor(P, s, true, nullptr);
+  P.M = M;
+  P.eval_idx = idx;
+  int rmax = 1;
+  for (int k = 0; k <= s.d; ++k)
+    rmax = std::max(rmax, s.r[k]);
+  P.rcap = (rmax + 31) / 32 * 32;
+  if (P.rcap > 1536)
+    return fail(TTG_ERR_NO_SPACE, "eval_batch: ranks above 1536 are not served");
+  TTG_CUDA(eval_smem_optin(P.rcap));
+  // layout: [arena | slots | tts | idx] prefix, then [out | bad].
+  size_t o = 0;
+  P.off_arena = o;
+  o = align256(o + sizeof(double) * static_cast<size_t>(P.arena_doubles));
+  P.off_slots = o;
+  o = align256(o + sizeof(CoreSlot) * P.slots.size());
+  P.off_tts = o;
+  o = align256(o + sizeof(TTInfo) * P.tts.size());
+  P.off_order = o;
+  const size_t table_end = o;
+  P.off_idx = o;
+  o = align256(o + sizeof(int32_t) * static_cast<size_t>(M) * s.d);
+  P.prefix_bytes = o;
+  P.off_out = o;
+  o = align256(o + sizeof(double) * static_cast<size_t>(std::max<int64_t>(M, 1)));
+  P.off_bad = o;
+  o = align256(o + 256);
+  P.total_bytes = o;
+  TTG_CUDA(P.dev.ensure(P.total_bytes));
+  TTG_CUDA(P.host.ensure(table_end));
+  char* h = static_cast<char*>(P.host.p);
+  std::memset(h, 0, table_end);
+  double* arena = reinterpret_cast<double*>(h + P.off_arena);
+  for (int k = 0; k < s.d; ++k)
+    std::memcpy(arena + P.slots[k].off, s.data + s.src_off[k],
+                sizeof(double) * static_cast<size_t>(s.size[k]));
+  std::memcpy(h + P.off_slots, P.slots.data(), sizeof(CoreSlot) * P.slots.size());
+  std::memcpy(h + P.off_tts, P.tts.data(), sizeof(TTInfo) * P.tts.size());
+  P.h2d = static_cast<int64_t>(table_end + sizeof(int32_t) * static_cast<size_t>(M) * s.d);
+  P.d2h = static_cast<int64_t>(sizeof(double) * M + sizeof(int));
+  return TTG_OK;
+}
+
+static int32_t eval_upload(ttg_plan& P, cudaStream_t st)
+{
+  char* d = static_cast<char*>(P.dev.p);
+  TTG_CUDA(cudaMemcpyAsync(d, P.host.p, P.off_order, cudaMemcpyHostToDevice, st));
+  if (P.M > 0)
+    TTG_CUDA(cudaMemcpyAsync(d + P.off_idx, P.eval_idx,
+                             sizeof(int32_t) * static_cast<size_t>(P.M) * P.shapes[0].d,
+                             cudaMemcpyHostToDevice, st));
+  return TTG_OK;
+}
+
+int32_t ttg_plan_create_eval(const ttg_tensor* a, const int32_t* idx, int32_t M, ttg_plan** plan)
+{
+  g_err.clear();
+  if (!plan)
+    return fail(TTG_ERR_ARG, "null plan");
+  if (int32_t st = need_device())
+    return st;
+  auto* P = new ttg_plan;
+  if (int32_t st = build_eval_plan(*P, a, idx, M))
+  {
+    delete P;
+    return st;
+  }
+  *plan = P;
+  return TTG_OK;
+}
+
+int32_t ttg_eval_batch(const ttg_tensor* a, const int32_t* idx, int32_t M, double* out)
+{
+  g_err.clear();
+  if (!out && M > 0)
+    return fail(TTG_ERR_ARG, "eval_batch: null output");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_plan P;
+  if (int32_t st = build_eval_plan(P, a, idx, M))
+    return st;
+  if (M == 0)
+    return TTG_OK;
+  cudaStream_t st = lib_stream();
+  if (int32_t e = eval_upload(P, st))
+    return e;
+  if (int32_t e = plan_run(P, st))
+    return e;
+  return ttg_plan_download(&P, st, nullptr, out, nullptr);
+}
+
+int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out)
+{
+  g_err.clear();
+  if (!out)
+    return fail(TTG_ERR_ARG, "inner: null output");
+  Shape A, B;
+  if (int32_t st = describe(a, "inner", A))
+    return st;
+  if (int32_t st = describe(b, "inner", B))
+    return st;
+  if (A.d != B.d)
+    return fail(TTG_ERR_SHAPE, "tt::inner: rank-d mismatch (a.d=" + std::to_string(A.d) +
+                                   ", b.d=" + std::to_string(B.d) + ")");
+  for (int k = 0; k < A.d; ++k)
+    if (A.mode(k) != B.mode(k))
+      return fail(TTG_ERR_SHAPE, "tt::inner: mode-size mismatch at axis " + std::to_string(k));
+  if (A.d == 0)
+  {
+    *out = 0.0;
+    return TTG_OK;
+  }
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_plan P;
+  P.shapes = {A, B};
+  add_tensor(P, A, true, nullptr);
+  add_tensor(P, B, true, nullptr);
+  int64_t env = 1, tmp = 1;
+  for (int k = 0; k < A.d; ++k)
+  {
+    env = std::max(env, static_cast<int64_t>(A.r[k + 1]) * B.r[k + 1]);
+    env = std::max(env, static_cast<int64_t>(A.r[k]) * B.r[k]);
+    tmp = std::max(tmp, static_cast<int64_t>(B.r[k]) * A.mode(k) * A.r[k + 1]);
+  }
+  env = a32(env);
+  P.scratch_stride = 2 * env + a32(tmp) + 32;
+  P.grid = 1;
+  P.job_kind = -1;
+  if (int32_t st = layout_and_alloc(P))
+    return st;
+  cudaStream_t st = lib_stream();
+  if (int32_t e = plan_upload(P, st))
+    return e;
+  char* d = static_cast<char*>(P.dev.p);
+  double* scratch = reinterpret_cast<double*>(d + P.off_scratch);
+  const CoreSlot* S = reinterpret_cast<const CoreSlot*>(d + P.off_slots);
+  launch_inner(reinterpret_cast<double*>(d + P.off_arena), S + P.tts[0].first,
+               S + P.tts[1].first, A.d, scratch, env, scratch + P.scratch_stride - 8, st);
+  g_launches += 1;
+  TTG_CUDA(cudaGetLastError());
+  TTG_CUDA(cudaMemcpyAsync(out, scratch + P.scratch_stride - 8, sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+  TTG_CUDA(cudaStreamSynchronize(st));
+  return TTG_OK;
+}
+
+int32_t ttg_norm(const ttg_tensor* a, double* out)
+{
+  double s = 0.0;
+  const int32_t st = ttg_inner(a, a, &s);
+  if (st)
+    return st;
+  *out = std::sqrt(std::max(s, 0.0));
+  return TTG_OK;
+}
+
+}  // extern "C"

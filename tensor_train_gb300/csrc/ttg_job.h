@@ -1,0 +1,113 @@
+// Device-side job tables shared by the host runtime and the kernels.
+//
+// HBM layout of a job: one arena of FP64 core slots.  Slot capacity is the
+// core's input size; rounding never grows a core (ranks only shrink along a
+// sweep), so every step writes its result back into the slot it came from.
+// The tables below are small and live next to the arena.
+#pragma once
+
+#include <cstdint>
+
+#if defined(__CUDACC__)
+#define TTG_HD __host__ __device__
+#else
+#define TTG_HD
+#endif
+
+namespace ttg
+{
+
+// Scratch sizes (doubles) of the sweep steps.  The host sizes each CTA's
+// slab with these functions evaluated at the input dimensions (upper bounds:
+// ranks only shrink during a sweep) and the device checks the same functions
+// at the actual dimensions before every step, so a step can never run past
+// its slab.  Each bump allocation is rounded up to 32 doubles (256 bytes).
+TTG_HD inline int64_t a32(int64_t n) { return (n + 31) & ~static_cast<int64_t>(31); }
+TTG_HD inline int64_t imax64(int64_t a, int64_t b) { return a > b ? a : b; }
+
+// left_svd on an (h x c) matrix, all three branches.
+TTG_HD inline int64_t need_left_svd(int64_t h, int64_t c)
+{
+  return 2 * a32(h * c) + 4 * a32(c * c) + 2 * a32(h * h) + 4 * a32(imax64(h, c));
+}
+// right_qr_step on a core (r, w = n*rp) with previous core of h_prev rows.
+TTG_HD inline int64_t need_right_qr(int64_t r, int64_t w, int64_t h_prev)
+{
+  return a32(w * r) + a32(r) + a32(r * r) + a32(h_prev * r);
+}
+// left_qr_step on a core (h = r*n, rp) with next core of w_next columns.
+TTG_HD inline int64_t need_left_qr(int64_t h, int64_t rp, int64_t w_next)
+{
+  return a32(h * rp) + a32(rp) + a32(rp * rp) + a32(rp * w_next);
+}
+TTG_HD inline int64_t need_svd_step(int64_t h, int64_t c, int64_t w_next)
+{
+  return a32(c * w_next) + need_left_svd(h, c);
+}
+TTG_HD inline int64_t need_svd_step_right(int64_t w, int64_t r, int64_t h_prev)
+{
+  return a32(h_prev * r) + need_left_svd(w, r);
+}
+// One streaming step: F buffer capacity fcap, F rows alpha, operator core
+// (a, m, p, b), operand core (sx, p*nout, bx).
+TTG_HD inline int64_t need_stream_step(int64_t fcap, int64_t alpha, int64_t a, int64_t m,
+                                       int64_t p, int64_t b, int64_t sx, int64_t nout,
+                                       int64_t bx)
+{
+  const int64_t g1p = alpha * m * b * sx * p;
+  const int64_t c2 = alpha * m * b * nout * bx;
+  return a32(fcap) + a32(alpha * sx * a) + a32(alpha * sx * m * p * b) + a32(g1p) + 2 * a32(c2) +
+         need_left_svd(alpha * m * nout, b * bx);
+}
+
+struct CoreSlot
+{
+  int64_t off;  // slot start in the arena (doubles)
+  int32_t n;    // mode size as stored (n, or m*n for a TT-matrix core)
+  int32_t r;    // current left rank (updated by the sweeps)
+  int32_t rp;   // current right rank
+  int32_t m;    // row mode of a TT-matrix core (0 for a TT core)
+};
+
+struct TTInfo
+{
+  int32_t first;   // index of core 0 in the slot table
+  int32_t d;
+  int32_t status;  // ttg_status
+  int32_t sweeps;  // largest Jacobi sweep count met
+  double norm;     // ||T|| computed by the sweep
+  double delta;    // truncation threshold used
+};
+
+enum JobKind : int32_t
+{
+  kJobRound = 0,          // round (gauge none): R->L QR, L->R SVD, balance
+  kJobRoundRight = 1,     // round_right_canonical: L->R QR, R->L SVD
+  kJobRightOrth = 2,      // right_orthogonalize only
+  kJobStreamMatvec = 3,   // build_streaming_matvec (pairs of TTs)
+  kJobStreamMatmat = 4,   // build_streaming_matmat
+};
+
+struct RoundJob
+{
+  double* arena;
+  CoreSlot* slots;
+  TTInfo* tts;
+  const int32_t* order;  // processing order (longest first)
+  int32_t ntt;           // number of work items
+  int32_t kind;
+  double* scratch;
+  int64_t scratch_stride;  // doubles per CTA
+  int32_t* queue;          // work counter (reset before each run)
+  double eps;
+  int32_t max_rank;
+  int32_t max_sweeps;
+  // Streaming jobs: item i rounds the product of TT a_idx[i] (operator) and
+  // b_idx[i] (operand) into output TT out_idx[i].  Row/col modes of the
+  // operator cores come from CoreSlot::m and n/m.
+  const int32_t* a_idx;
+  const int32_t* b_idx;
+  const int32_t* out_idx;
+};
+
+}  // namespace ttg

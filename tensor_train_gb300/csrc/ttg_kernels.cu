@@ -1,0 +1,856 @@
+// FP64 TT sweep kernels for sm_103a.
+//
+// One CTA owns one tensor train for a whole sweep (persistent CTAs pull
+// work items from an atomic queue, longest first).  Cores stay in their HBM
+// slots for the whole call; each step reads a core, factors it in the CTA's
+// scratch slab and writes the result back into the same slot.  Structure
+// of a step follows the reference:
+//   right_qr_step / left_qr_step     detail/orthogonalize.hpp:35-100
+//   svd_step / svd_step_right        detail/truncate.hpp:61-166
+//   detail::round                    round/tt_round.hpp:36-127
+//   round_right_canonical            round/tt_round.hpp:151-183
+//   build_streaming_matvec/matmat    detail/streaming_apply.hpp:39-202
+//   fused_matvec/matmat_core         detail/fused_apply_core.hpp:33-272
+//   matvec_core / matmat_core        apply/tt_matrix_apply.hpp:40-224
+//   eval_at / eval_batch             algebra/tt_eval.hpp:32-112
+//   inner (contract_inner_step)      algebra/tt_inner.hpp:33-47,
+//                                    detail/contract.hpp:155-205
+#include <cuda_runtime.h>
+
+#include "ttg_device.cuh"
+#include "ttg_job.h"
+#include "ttg_kernels.h"
+
+namespace ttg
+{
+
+namespace
+{
+
+constexpr int kStatusOk = 0;
+constexpr int kStatusNan = 5;
+constexpr int kStatusNotConverged = 6;
+constexpr int kStatusNoSpace = 11;
+
+// Bump allocator over the CTA's scratch slab (256-byte aligned chunks).
+struct Bump
+{
+  double* p;
+  __device__ double* take(int64_t n)
+  {
+    double* r = p;
+    p += (n + 31) & ~static_cast<int64_t>(31);
+    return r;
+  }
+};
+
+__device__ __forceinline__ bool finite(double x) { return isfinite(x); }
+
+// Records a status on the TT (first error wins) -- thread 0 only.
+__device__ void set_status(TTInfo& T, int st)
+{
+  if (threadIdx.x == 0 && T.status == kStatusOk)
+    T.status = st;
+}
+
+// QR of X (h x c).  Q -> W (h x k, column-major, ld h), R -> R (k x c,
+// column-major, ld k), k = min(h, c).
+__device__ int qr_factor(View X, int h, int c, double* W, double* tau, double* R, CtaShared& sh)
+{
+  cta_copy_to_colmajor(W, h, X, h, c);
+  __syncthreads();
+  cta_householder_qr(W, h, c, h, tau, sh);
+  const int k = h < c ? h : c;
+  cta_extract_r(R, W, k, c, h);
+  cta_form_q(W, h, k, h, tau);
+  return k;
+}
+
+// Truncated SVD of X (h x c) = U S V^T, as used by svd_step
+// (detail/truncate.hpp:61-99): returns r_new and
+//   Ut (h x r_new, column-major, ld h): leading left singular vectors,
+//   F  (r_new x c, row-major):         diag(s) * V^T leading rows.
+// Branches as the reference: QR-condense when h >= 2c (truncate.hpp:76-85);
+// otherwise decompose X directly -- by columns when h >= c, by rows (the
+// transpose, accumulating V) when h < c.
+__device__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
+                        Bump bump, double** Ut_out, double** F_out, TTInfo& T, CtaShared& sh)
+{
+  double* sig;
+  double* sorted;
+  int* ord;
+  double* U;
+  double* F;
+  int sweeps = 0, conv = 1;
+  if (h >= 2 * c)
+  {
+    double* W = bump.take(static_cast<int64_t>(h) * c);
+    double* tau = bump.take(c);
+    double* R = bump.take(static_cast<int64_t>(c) * c);
+    double* A = bump.take(static_cast<int64_t>(c) * c);
+    sig = bump.take(c);
+    sorted = bump.take(c);
+    ord = reinterpret_cast<int*>(bump.take(c));
+    double* Uc = bump.take(static_cast<int64_t>(c) * c);
+    U = bump.take(static_cast<int64_t>(h) * c);
+    F = bump.take(static_cast<int64_t>(c) * c);
+    cta_copy_to_colmajor(W, h, X, h, c);
+    __syncthreads();
+    cta_householder_qr(W, h, c, h, tau, sh);
+    cta_extract_r(R, W, c, c, h);
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(c) * c; t += blockDim.x)
+      A[t] = R[t];
+    __syncthreads();
+    sweeps = cta_jacobi(A, c, c, c, nullptr, 0, max_sweeps, &conv, sh);
+    cta_col_norms(A, c, c, c, sig);
+    cta_argsort_desc(sig, c, ord, sorted);
+    if (threadIdx.x == 0)
+      sh.ival[0] = trunc_rank_serial(sorted, c, delta, max_rank);
+    __syncthreads();
+    const int r_new = sh.ival[0];
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(c) * r_new; t += blockDim.x)
+    {
+      const int i = static_cast<int>(t % c), jj = static_cast<int>(t / c);
+      const double s = sorted[jj];
+      Uc[t] = s > 0.0 ? A[i + static_cast<int64_t>(ord[jj]) * c] / s : 0.0;
+    }
+    __syncthreads();
+    // F = Uc^T R  (= diag(s) V^T restricted to the kept rows).
+    cta_gemm(r_new, c, c, View{Uc, c, 1}, View{R, 1, c}, F, c, 1, sh);
+    // U = Q [Uc; 0] by applying the reflectors.
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
+    {
+      const int i = static_cast<int>(t % h), jj = static_cast<int>(t / h);
+      U[t] = i < c ? Uc[i + static_cast<int64_t>(jj) * c] : 0.0;
+    }
+    __syncthreads();
+    cta_apply_q(W, h, c, h, tau, U, r_new, h);
+    if (threadIdx.x == 0)
+    {
+      if (!finite(sorted[0]))
+        set_status(T, kStatusNan);
+      if (!conv)
+        set_status(T, kStatusNotConverged);
+      if (sweeps > T.sweeps)
+        T.sweeps = sweeps;
+    }
+    __syncthreads();
+    *Ut_out = U;
+    *F_out = F;
+    return r_new;
+  }
+  if (h >= c)
+  {
+    double* A = bump.take(static_cast<int64_t>(h) * c);
+    sig = bump.take(c);
+    sorted = bump.take(c);
+    ord = reinterpret_cast<int*>(bump.take(c));
+    U = bump.take(static_cast<int64_t>(h) * c);
+    F = bump.take(static_cast<int64_t>(c) * c);
+    cta_copy_to_colmajor(A, h, X, h, c);
+    __syncthreads();
+    sweeps = cta_jacobi(A, h, c, h, nullptr, 0, max_sweeps, &conv, sh);
+    cta_col_norms(A, h, c, h, sig);
+    cta_argsort_desc(sig, c, ord, sorted);
+    if (threadIdx.x == 0)
+      sh.ival[0] = trunc_rank_serial(sorted, c, delta, max_rank);
+    __syncthreads();
+    const int r_new = sh.ival[0];
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
+    {
+      const int i = static_cast<int>(t % h), jj = static_cast<int>(t / h);
+      const double s = sorted[jj];
+      U[t] = s > 0.0 ? A[i + static_cast<int64_t>(ord[jj]) * h] / s : 0.0;
+    }
+    __syncthreads();
+    // F = U^T X.
+    cta_gemm(r_new, c, h, View{U, h, 1}, X, F, c, 1, sh);
+    if (threadIdx.x == 0)
+    {
+      if (!finite(sorted[0]))
+        set_status(T, kStatusNan);
+      if (!conv)
+        set_status(T, kStatusNotConverged);
+      if (sweeps > T.sweeps)
+        T.sweeps = sweeps;
+    }
+    __syncthreads();
+    *Ut_out = U;
+    *F_out = F;
+    return r_new;
+  }
+  // h < c: Jacobi on X^T (c x h), V (h x h) accumulates the rotations and
+  // becomes U; the rotated columns are the rows of diag(s) V^T.
+  double* A = bump.take(static_cast<int64_t>(c) * h);
+  double* V = bump.take(static_cast<int64_t>(h) * h);
+  sig = bump.take(h);
+  sorted = bump.take(h);
+  ord = reinterpret_cast<int*>(bump.take(h));
+  U = bump.take(static_cast<int64_t>(h) * h);
+  F = bump.take(static_cast<int64_t>(h) * c);
+  cta_copy_to_colmajor(A, c, transposed(X), c, h);
+  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * h; t += blockDim.x)
+    V[t] = (t % h == t / h) ? 1.0 : 0.0;
+  __syncthreads();
+  sweeps = cta_jacobi(A, c, h, c, V, h, max_sweeps, &conv, sh);
+  cta_col_norms(A, c, h, c, sig);
+  cta_argsort_desc(sig, h, ord, sorted);
+  if (threadIdx.x == 0)
+    sh.ival[0] = trunc_rank_serial(sorted, h, delta, max_rank);
+  __syncthreads();
+  const int r_new = sh.ival[0];
+  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
+  {
+    const int i = static_cast<int>(t % h), jj = static_cast<int>(t / h);
+    U[t] = V[i + static_cast<int64_t>(ord[jj]) * h];
+  }
+  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(r_new) * c; t += blockDim.x)
+  {
+    const int jj = static_cast<int>(t / c), j = static_cast<int>(t % c);
+    F[t] = A[j + static_cast<int64_t>(ord[jj]) * c];
+  }
+  if (threadIdx.x == 0)
+  {
+    if (!finite(sorted[0]))
+      set_status(T, kStatusNan);
+    if (!conv)
+      set_status(T, kStatusNotConverged);
+    if (sweeps > T.sweeps)
+      T.sweeps = sweeps;
+  }
+  __syncthreads();
+  *Ut_out = U;
+  *F_out = F;
+  return r_new;
+}
+
+__device__ void cta_copy(double* dst, const double* src, int64_t n)
+{
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x)
+    dst[t] = src[t];
+  __syncthreads();
+}
+
+__device__ void set_ranks(CoreSlot& s, int r, int rp)
+{
+  if (threadIdx.x == 0)
+  {
+    s.r = r;
+    s.rp = rp;
+  }
+}
+
+// right_qr_step (detail/orthogonalize.hpp:63-100): QR of M^T (n*rp x r);
+// r_eff = min(n*rp, r); L = R^T absorbed into prev.
+__device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bump, CtaShared& sh)
+{
+  const int r = cur.r, n = cur.n, rp = cur.rp;
+  const int w = n * rp;
+  const int hp = prev.r * prev.n;
+  double* cs = ar + cur.off;
+  double* ps = ar + prev.off;
+  double* W = bump.take(static_cast<int64_t>(w) * r);
+  double* tau = bump.take(r);
+  double* R = bump.take(static_cast<int64_t>(r) * r);
+  double* P = bump.take(static_cast<int64_t>(hp) * r);
+  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sh);
+  // prev (hp x k) = left_unfold(prev) (hp x r) * L, L(a, e) = R(e, a).
+  cta_gemm(hp, k, r, View{ps, r, 1}, View{R, k, 1}, P, k, 1, sh);
+  cta_copy(ps, P, static_cast<int64_t>(hp) * k);
+  cta_copy(cs, W, static_cast<int64_t>(w) * k);
+  set_ranks(cur, k, rp);
+  set_ranks(prev, prev.r, k);
+  __syncthreads();
+}
+
+// left_qr_step (detail/orthogonalize.hpp:35-60).
+__device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bump, CtaShared& sh)
+{
+  const int r = cur.r, n = cur.n, rp = cur.rp;
+  const int h = r * n;
+  const int wn = next.n * next.rp;
+  double* cs = ar + cur.off;
+  double* ns = ar + next.off;
+  double* W = bump.take(static_cast<int64_t>(h) * rp);
+  double* tau = bump.take(rp);
+  double* R = bump.take(static_cast<int64_t>(rp) * rp);
+  double* P = bump.take(static_cast<int64_t>(rp) * wn);
+  const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sh);
+  // next (k x wn) = R (k x rp) * right_unfold(next) (rp x wn).
+  cta_gemm(k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, P, wn, 1, sh);
+  cta_copy(ns, P, static_cast<int64_t>(k) * wn);
+  // cur row-major (h x k) <- Q column-major.
+  cta_copy_to_rowmajor(cs, k, View{W, 1, h}, h, k);
+  set_ranks(cur, r, k);
+  set_ranks(next, k, next.rp);
+  __syncthreads();
+}
+
+// svd_step (detail/truncate.hpp:61-99).
+__device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& next,
+                         double delta, Bump bump, TTInfo& T, CtaShared& sh)
+{
+  const int r = cur.r, n = cur.n, c = cur.rp;
+  const int h = r * n;
+  const int wn = next.n * next.rp;
+  double* cs = ar + cur.off;
+  double* ns = ar + next.off;
+  double* P = bump.take(static_cast<int64_t>(c) * wn);
+  double *U, *F;
+  const int r_new = left_svd(View{cs, c, 1}, h, c, delta, job.max_rank, job.max_sweeps, bump, &U,
+                             &F, T, sh);
+  cta_gemm(r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, P, wn, 1, sh);
+  cta_copy(ns, P, static_cast<int64_t>(r_new) * wn);
+  cta_copy_to_rowmajor(cs, r_new, View{U, 1, h}, h, r_new);
+  set_ranks(cur, r, r_new);
+  set_ranks(next, r_new, next.rp);
+  __syncthreads();
+}
+
+// svd_step_right (detail/truncate.hpp:114-166) as a left step on M^T.
+__device__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& prev,
+                               double delta, Bump bump, TTInfo& T, CtaShared& sh)
+{
+  const int r = cur.r, n = cur.n, rp = cur.rp;
+  const int w = n * rp;
+  const int hp = prev.r * prev.n;
+  double* cs = ar + cur.off;
+  double* ps = ar + prev.off;
+  double* P = bump.take(static_cast<int64_t>(hp) * r);
+  double *U, *F;
+  const int r_new = left_svd(View{cs, 1, w}, w, r, delta, job.max_rank, job.max_sweeps, bump, &U,
+                             &F, T, sh);
+  // prev (hp x r_new) = left_unfold(prev) (hp x r) * F^T.
+  cta_gemm(hp, r_new, r, View{ps, r, 1}, View{F, 1, r}, P, r_new, 1, sh);
+  cta_copy(ps, P, static_cast<int64_t>(hp) * r_new);
+  cta_copy(cs, U, static_cast<int64_t>(w) * r_new);
+  set_ranks(cur, r_new, rp);
+  set_ranks(prev, prev.r, r_new);
+  __syncthreads();
+}
+
+__device__ double core_norm(const double* p, int64_t n, CtaShared& sh)
+{
+  double s = 0.0;
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x)
+    s += p[t] * p[t];
+  return sqrt(cta_sum(s, sh));
+}
+
+__device__ int64_t core_size(const CoreSlot& s)
+{
+  return static_cast<int64_t>(s.r) * s.n * s.rp;
+}
+
+// make_rank1_zero_tt (detail/shape_check.hpp:176-188).
+__device__ void zero_tt(double* ar, CoreSlot* S, int d)
+{
+  for (int k = 0; k < d; ++k)
+  {
+    for (int i = threadIdx.x; i < S[k].n; i += blockDim.x)
+      ar[S[k].off + i] = 0.0;
+    set_ranks(S[k], 1, 1);
+  }
+  __syncthreads();
+}
+
+// Norm balancing (round/tt_round.hpp:65-124).
+__device__ void balance(double* ar, CoreSlot* S, int d, Bump bump, CtaShared& sh)
+{
+  int64_t total = 0;
+  for (int k = 0; k < d - 1; ++k)
+    total += S[k].rp;
+  double* cn = bump.take(total + 1);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double my_log = 0.0, my_cnt = 0.0;
+  int64_t base = 0;
+  for (int k = 0; k < d - 1; ++k)
+  {
+    const int h = S[k].r * S[k].n, c = S[k].rp;
+    const double* p = ar + S[k].off;
+    for (int col = w; col < c; col += kWarps)
+    {
+      double s = 0.0;
+      for (int i = lane; i < h; i += 32)
+        s += p[static_cast<int64_t>(i) * c + col] * p[static_cast<int64_t>(i) * c + col];
+      s = warp_sum(s);
+      const double nc = sqrt(s);
+      if (lane == 0)
+      {
+        cn[base + col] = nc;
+        if (nc > 0.0)
+        {
+          my_log += log(nc);
+          my_cnt += 1.0;
+        }
+      }
+    }
+    base += c;
+  }
+  const double tot_log = cta_sum(my_log, sh);
+  const double tot_cnt = cta_sum(my_cnt, sh);
+  if (tot_cnt <= 0.0)
+    return;
+  const double geo = exp(tot_log / tot_cnt);
+  base = 0;
+  int64_t prev_base = 0;
+  for (int k = 0; k < d; ++k)
+  {
+    const int r = S[k].r, n = S[k].n, c = S[k].rp;
+    double* p = ar + S[k].off;
+    const int64_t sz = static_cast<int64_t>(r) * n * c;
+    for (int64_t t = threadIdx.x; t < sz; t += blockDim.x)
+    {
+      const int a = static_cast<int>(t / (static_cast<int64_t>(n) * c));
+      const int b = static_cast<int>(t % c);
+      double x = p[t];
+      if (k >= 1)
+      {
+        const double nr = cn[prev_base + a];
+        if (nr > 0.0)
+          x /= geo / nr;
+      }
+      if (k <= d - 2)
+      {
+        const double nc = cn[base + b];
+        if (nc > 0.0)
+          x *= geo / nc;
+      }
+      p[t] = x;
+    }
+    if (k <= d - 2)
+    {
+      prev_base = base;
+      base += c;
+    }
+  }
+  __syncthreads();
+}
+
+// Scratch guard: the step needs `need` doubles of the CTA's slab.
+__device__ bool fits(const RoundJob& job, int64_t need, TTInfo& T)
+{
+  if (need <= job.scratch_stride)
+    return true;
+  set_status(T, kStatusNoSpace);
+  __syncthreads();
+  return false;
+}
+
+__device__ int64_t balance_need(const CoreSlot* S, int d)
+{
+  int64_t total = 0;
+  for (int k = 0; k < d - 1; ++k)
+    total += S[k].rp;
+  return a32(total + 1);
+}
+
+__device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShared& sh)
+{
+  TTInfo& T = job.tts[tti];
+  const int d = T.d;
+  CoreSlot* S = job.slots + T.first;
+  double* ar = job.arena;
+  if (d <= 1)
+    return;
+  if (job.kind == kJobRound || job.kind == kJobRightOrth)
+  {
+    for (int k = d - 1; k >= 1; --k)
+    {
+      if (!fits(job, need_right_qr(S[k].r, static_cast<int64_t>(S[k].n) * S[k].rp,
+                                   static_cast<int64_t>(S[k - 1].r) * S[k - 1].n), T))
+        return;
+      right_qr_step(ar, S[k], S[k - 1], Bump{scratch}, sh);
+    }
+    if (job.kind == kJobRightOrth)
+      return;
+    const double nrm = core_norm(ar + S[0].off, core_size(S[0]), sh);
+    if (threadIdx.x == 0)
+      T.norm = nrm;
+    if (!isfinite(nrm))
+    {
+      set_status(T, kStatusNan);
+      return;
+    }
+    if (nrm == 0.0)
+    {
+      zero_tt(ar, S, d);
+      return;
+    }
+    const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+    if (threadIdx.x == 0)
+      T.delta = delta;
+    for (int k = 0; k < d - 1; ++k)
+    {
+      if (!fits(job, need_svd_step(static_cast<int64_t>(S[k].r) * S[k].n, S[k].rp,
+                                   static_cast<int64_t>(S[k + 1].n) * S[k + 1].rp), T))
+        return;
+      svd_step(job, ar, S[k], S[k + 1], delta, Bump{scratch}, T, sh);
+    }
+    if (!fits(job, balance_need(S, d), T))
+      return;
+    balance(ar, S, d, Bump{scratch}, sh);
+    return;
+  }
+  // round_right_canonical.
+  for (int k = 0; k < d - 1; ++k)
+  {
+    if (!fits(job, need_left_qr(static_cast<int64_t>(S[k].r) * S[k].n, S[k].rp,
+                                static_cast<int64_t>(S[k + 1].n) * S[k + 1].rp), T))
+      return;
+    left_qr_step(ar, S[k], S[k + 1], Bump{scratch}, sh);
+  }
+  const double nrm = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
+  if (threadIdx.x == 0)
+    T.norm = nrm;
+  if (!isfinite(nrm))
+  {
+    set_status(T, kStatusNan);
+    return;
+  }
+  if (nrm == 0.0)
+  {
+    zero_tt(ar, S, d);
+    return;
+  }
+  const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+  if (threadIdx.x == 0)
+    T.delta = delta;
+  for (int k = d - 1; k >= 1; --k)
+  {
+    if (!fits(job, need_svd_step_right(static_cast<int64_t>(S[k].n) * S[k].rp, S[k].r,
+                                       static_cast<int64_t>(S[k - 1].r) * S[k - 1].n), T))
+      return;
+    svd_step_right(job, ar, S[k], S[k - 1], delta, Bump{scratch}, T, sh);
+  }
+}
+
+// build_streaming_matvec / build_streaming_matmat
+// (detail/streaming_apply.hpp:39-202) for one (operator, operand) pair.
+__device__ void stream_tt(const RoundJob& job, int item, double* scratch, CtaShared& sh)
+{
+  double* ar = job.arena;
+  TTInfo& TA = job.tts[job.a_idx[item]];
+  TTInfo& TX = job.tts[job.b_idx[item]];
+  TTInfo& TO = job.tts[job.out_idx[item]];
+  CoreSlot* SA = job.slots + TA.first;
+  CoreSlot* SX = job.slots + TX.first;
+  CoreSlot* SO = job.slots + TO.first;
+  const int d = TA.d;
+  for (int k = d - 1; k >= 1; --k)
+  {
+    if (!fits(job, need_right_qr(SA[k].r, static_cast<int64_t>(SA[k].n) * SA[k].rp,
+                                 static_cast<int64_t>(SA[k - 1].r) * SA[k - 1].n), TO))
+      return;
+    right_qr_step(ar, SA[k], SA[k - 1], Bump{scratch}, sh);
+  }
+  for (int k = d - 1; k >= 1; --k)
+  {
+    if (!fits(job, need_right_qr(SX[k].r, static_cast<int64_t>(SX[k].n) * SX[k].rp,
+                                 static_cast<int64_t>(SX[k - 1].r) * SX[k - 1].n), TO))
+      return;
+    right_qr_step(ar, SX[k], SX[k - 1], Bump{scratch}, sh);
+  }
+  const double nA = core_norm(ar + SA[0].off, core_size(SA[0]), sh);
+  const double nX = core_norm(ar + SX[0].off, core_size(SX[0]), sh);
+  const double nrm = nA * nX;
+  if (threadIdx.x == 0)
+    TO.norm = nrm;
+  if (!isfinite(nrm))
+  {
+    set_status(TO, kStatusNan);
+    return;
+  }
+  if (nrm == 0.0)
+  {
+    zero_tt(ar, SO, d);
+    return;
+  }
+  const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+  if (threadIdx.x == 0)
+    TO.delta = delta;
+  // Persistent F buffer at the front of the slab; per-step scratch after it.
+  // F holds r_new x (b*bx) with r_new <= b*bx.
+  int64_t fcap = 1;
+  for (int k = 0; k < d; ++k)
+  {
+    const int64_t cap = static_cast<int64_t>(SA[k].rp) * SX[k].rp;
+    fcap = fcap > cap * cap ? fcap : cap * cap;
+  }
+  double* Fbuf = scratch;
+  Bump base{scratch + ((fcap + 31) & ~static_cast<int64_t>(31))};
+  if (threadIdx.x == 0)
+    Fbuf[0] = 1.0;
+  int alpha = 1;
+  __syncthreads();
+  for (int k = 0; k < d; ++k)
+  {
+    Bump bump = base;
+    const int a = SA[k].r, b = SA[k].rp;
+    const int m = SA[k].m;
+    const int p = SA[k].n / m;
+    const int sx = SX[k].r, bx = SX[k].rp;
+    const int nout = SX[k].n / p;
+    if (!fits(job, need_stream_step(fcap, alpha, a, m, p, b, sx, nout, bx), TO))
+      return;
+    const int64_t mpb = static_cast<int64_t>(m) * p * b;
+    // Fp (alpha*sx x a): Fp[(al*sx + ax), aa] = F[al, aa*sx + ax].
+    double* Fp = bump.take(static_cast<int64_t>(alpha) * sx * a);
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(alpha) * sx * a; t += blockDim.x)
+    {
+      const int aa = static_cast<int>(t % a);
+      const int64_t row = t / a;
+      const int al = static_cast<int>(row / sx), ax = static_cast<int>(row % sx);
+      Fp[t] = Fbuf[static_cast<int64_t>(al) * a * sx + static_cast<int64_t>(aa) * sx + ax];
+    }
+    __syncthreads();
+    // G1 (alpha*sx x m*p*b) = Fp * A_k.
+    double* G1 = bump.take(static_cast<int64_t>(alpha) * sx * mpb);
+    cta_gemm(alpha * sx, static_cast<int>(mpb), a, View{Fp, a, 1}, View{ar + SA[k].off, mpb, 1},
+             G1, mpb, 1, sh);
+    // G1p ((al, i, bb) x (ax, q)).
+    const int64_t g1p_rows = static_cast<int64_t>(alpha) * m * b;
+    const int64_t g1p_cols = static_cast<int64_t>(sx) * p;
+    double* G1p = bump.take(g1p_rows * g1p_cols);
+    for (int64_t t = threadIdx.x; t < g1p_rows * g1p_cols; t += blockDim.x)
+    {
+      const int64_t row = t / g1p_cols, col = t % g1p_cols;
+      const int bb = static_cast<int>(row % b);
+      const int i = static_cast<int>((row / b) % m);
+      const int al = static_cast<int>(row / (static_cast<int64_t>(b) * m));
+      const int ax = static_cast<int>(col / p), q = static_cast<int>(col % p);
+      G1p[t] = G1[(static_cast<int64_t>(al) * sx + ax) * mpb + (static_cast<int64_t>(i) * p + q) * b + bb];
+    }
+    __syncthreads();
+    // C2 ((al,i,bb) x (j,bx')) = G1p * X_k.
+    const int64_t c2_cols = static_cast<int64_t>(nout) * bx;
+    double* C2 = bump.take(g1p_rows * c2_cols);
+    cta_gemm(static_cast<int>(g1p_rows), static_cast<int>(c2_cols), static_cast<int>(g1p_cols),
+             View{G1p, g1p_cols, 1}, View{ar + SX[k].off, c2_cols, 1}, C2, c2_cols, 1, sh);
+    // Cj (al, i, j, bb, bx') row-major.
+    double* Cj = C2;
+    if (nout > 1)
+    {
+      Cj = bump.take(g1p_rows * c2_cols);
+      for (int64_t t = threadIdx.x; t < g1p_rows * c2_cols; t += blockDim.x)
+      {
+        const int bxx = static_cast<int>(t % bx);
+        const int bb = static_cast<int>((t / bx) % b);
+        const int j = static_cast<int>((t / (static_cast<int64_t>(bx) * b)) % nout);
+        const int64_t ai = t / (static_cast<int64_t>(bx) * b * nout);  // al*m + i
+        Cj[t] = C2[(ai * b + bb) * c2_cols + static_cast<int64_t>(j) * bx + bxx];
+      }
+      __syncthreads();
+    }
+    const int hrows = alpha * m * nout;
+    const int ccols = b * bx;
+    double* os = ar + SO[k].off;
+    if (k == d - 1)
+    {
+      cta_copy(os, Cj, static_cast<int64_t>(hrows) * ccols);
+      set_ranks(SO[k], alpha, ccols);
+      __syncthreads();
+      break;
+    }
+    double *U, *F;
+    const int r_new = left_svd(View{Cj, ccols, 1}, hrows, ccols, delta, job.max_rank,
+                               job.max_sweeps, bump, &U, &F, TO, sh);
+    cta_copy_to_rowmajor(os, r_new, View{U, 1, hrows}, hrows, r_new);
+    cta_copy(Fbuf, F, static_cast<int64_t>(r_new) * ccols);
+    set_ranks(SO[k], alpha, r_new);
+    alpha = r_new;
+    __syncthreads();
+  }
+}
+
+}  // namespace
+
+__global__ void __launch_bounds__(kThreads) round_kernel(RoundJob job)
+{
+  __shared__ CtaShared sh;
+  double* scratch = job.scratch + static_cast<int64_t>(blockIdx.x) * job.scratch_stride;
+  for (;;)
+  {
+    if (threadIdx.x == 0)
+      sh.item = atomicAdd(job.queue, 1);
+    __syncthreads();
+    const int item = sh.item;
+    __syncthreads();
+    if (item >= job.ntt)
+      break;
+    if (job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat)
+      stream_tt(job, job.order[item], scratch, sh);
+    else
+      round_tt(job, job.order[item], scratch, sh);
+  }
+}
+
+// matvec_core / matmat_core (apply/tt_matrix_apply.hpp:40-224):
+// y(a*s+ax, i, j, b*sp+bx) = sum_q A(a, i, q, b) X(ax, q, j, bx), with j of
+// size nout (1 for matvec).  One thread per output element.
+__global__ void apply_core_kernel(const double* __restrict__ Ac, const double* __restrict__ Xc,
+                                  double* __restrict__ Y, int r, int m, int p, int rp, int s,
+                                  int nout, int sp)
+{
+  const int64_t total = static_cast<int64_t>(r) * s * m * nout * rp * sp;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < total;
+       t += static_cast<int64_t>(gridDim.x) * blockDim.x)
+  {
+    int64_t u = t;
+    const int bx = static_cast<int>(u % sp);
+    u /= sp;
+    const int b = static_cast<int>(u % rp);
+    u /= rp;
+    const int j = static_cast<int>(u % nout);
+    u /= nout;
+    const int i = static_cast<int>(u % m);
+    u /= m;
+    const int ax = static_cast<int>(u % s);
+    const int a = static_cast<int>(u / s);
+    double acc = 0.0;
+    for (int q = 0; q < p; ++q)
+      acc = fma(Ac[((static_cast<int64_t>(a) * m + i) * p + q) * rp + b],
+                Xc[((static_cast<int64_t>(ax) * p + q) * nout + j) * sp + bx], acc);
+    Y[t] = acc;
+  }
+}
+
+// eval_batch: one warp per multi-index; the running row vector lives in
+// shared memory (two buffers per warp of `rcap` doubles).
+__global__ void __launch_bounds__(kThreads) eval_kernel(const double* __restrict__ ar,
+                                                        const CoreSlot* __restrict__ S, int d,
+                                                        const int* __restrict__ idx, int64_t M,
+                                                        double* __restrict__ out, int rcap,
+                                                        int* __restrict__ bad)
+{
+  extern __shared__ double evbuf[];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double* v = evbuf + static_cast<int64_t>(w) * 2 * rcap;
+  double* vn = v + rcap;
+  const int64_t warps_total = static_cast<int64_t>(gridDim.x) * kWarps;
+  for (int64_t smp = blockIdx.x * static_cast<int64_t>(kWarps) + w; smp < M; smp += warps_total)
+  {
+    const int* ix = idx + smp * d;
+    int i0 = ix[0];
+    bool ok = (i0 >= 0 && i0 < S[0].n);
+    for (int k = 1; k < d; ++k)
+    {
+      const int ik = ix[k];
+      ok = ok && (ik >= 0 && ik < S[k].n);
+    }
+    if (!ok)
+    {
+      if (lane == 0)
+      {
+        out[smp] = __longlong_as_double(0x7ff8000000000000ll);
+        atomicExch(bad, 1);
+      }
+      continue;
+    }
+    {
+      const int r1 = S[0].rp;
+      const double* c0 = ar + S[0].off + static_cast<int64_t>(i0) * r1;
+      for (int b = lane; b < r1; b += 32)
+        v[b] = c0[b];
+    }
+    __syncwarp();
+    for (int k = 1; k < d; ++k)
+    {
+      const int r = S[k].r, n = S[k].n, rp = S[k].rp;
+      const int ik = ix[k];
+      const double* ck = ar + S[k].off + static_cast<int64_t>(ik) * rp;
+      const int64_t stride = static_cast<int64_t>(n) * rp;
+      for (int b0 = 0; b0 < rp; b0 += 32)
+      {
+        const int b = b0 + lane;
+        double acc = 0.0;
+        if (b < rp)
+          for (int a = 0; a < r; ++a)
+            acc = fma(v[a], ck[a * stride + b], acc);
+        if (b < rp)
+          vn[b] = acc;
+      }
+      __syncwarp();
+      double* t = v;
+      v = vn;
+      vn = t;
+    }
+    if (lane == 0)
+      out[smp] = v[0];
+    __syncwarp();
+  }
+}
+
+// inner (algebra/tt_inner.hpp:33-47): one CTA runs the left-to-right
+// environment chain of contract_inner_step (detail/contract.hpp:155-205).
+__global__ void __launch_bounds__(kThreads) inner_kernel(const double* __restrict__ ar,
+                                                         const CoreSlot* __restrict__ SA,
+                                                         const CoreSlot* __restrict__ SB, int d,
+                                                         double* scratch, int64_t env_cap,
+                                                         double* out)
+{
+  __shared__ CtaShared sh;
+  double* E = scratch;
+  double* En = scratch + env_cap;
+  double* tmp = scratch + 2 * env_cap;
+  if (threadIdx.x == 0)
+    E[0] = 1.0;
+  __syncthreads();
+  for (int k = 0; k < d; ++k)
+  {
+    const int ra = SA[k].r, n = SA[k].n, rap = SA[k].rp;
+    const int rb = SB[k].r, rbp = SB[k].rp;
+    const double* ca = ar + SA[k].off;
+    const double* cb = ar + SB[k].off;
+    // tmp (rb x n*rap) = E^T * right_unfold(ca).
+    cta_gemm(rb, n * rap, ra, View{E, 1, rb}, View{ca, static_cast<int64_t>(n) * rap, 1}, tmp,
+             static_cast<int64_t>(n) * rap, 1, sh);
+    // En (rap x rbp) = tmp_as^T (rap x rb*n) * left_unfold(cb) (rb*n x rbp).
+    cta_gemm(rap, rbp, rb * n, View{tmp, 1, rap}, View{cb, rbp, 1}, En, rbp, 1, sh);
+    double* t = E;
+    E = En;
+    En = t;
+  }
+  if (threadIdx.x == 0)
+    *out = E[0];
+}
+
+void launch_round(const RoundJob& job, int grid, cudaStream_t stream)
+{
+  round_kernel<<<grid, kThreads, 0, stream>>>(job);
+}
+
+void launch_apply_core(const double* A, const double* X, double* Y, int r, int m, int p, int rp,
+                       int s, int nout, int sp, cudaStream_t stream)
+{
+  const int64_t total = static_cast<int64_t>(r) * s * m * nout * rp * sp;
+  int64_t blocks = (total + 255) / 256;
+  if (blocks > 65535)
+    blocks = 65535;
+  if (blocks < 1)
+    blocks = 1;
+  apply_core_kernel<<<static_cast<int>(blocks), 256, 0, stream>>>(A, X, Y, r, m, p, rp, s, nout,
+                                                                  sp);
+}
+
+void launch_eval(const double* ar, const CoreSlot* S, int d, const int* idx, int64_t M,
+                 double* out, int rcap, int* bad, int grid, cudaStream_t stream)
+{
+  const size_t smem = static_cast<size_t>(kWarps) * 2 * rcap * sizeof(double);
+  eval_kernel<<<grid, kThreads, smem, stream>>>(ar, S, d, idx, M, out, rcap, bad);
+}
+
+void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int d,
+                  double* scratch, int64_t env_cap, double* out, cudaStream_t stream)
+{
+  inner_kernel<<<1, kThreads, 0, stream>>>(ar, SA, SB, d, scratch, env_cap, out);
+}
+
+cudaError_t eval_smem_optin(int rcap)
+{
+  const size_t smem = static_cast<size_t>(kWarps) * 2 * rcap * sizeof(double);
+  return cudaFuncSetAttribute(eval_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(smem));
+}
+
+}  // namespace ttg

@@ -1,0 +1,20 @@
+// Host-side launchers of the sweep, apply, eval and inner kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "ttg_job.h"
+
+namespace ttg
+{
+
+void launch_round(const RoundJob& job, int grid, cudaStream_t stream);
+void launch_apply_core(const double* A, const double* X, double* Y, int r, int m, int p, int rp,
+                       int s, int nout, int sp, cudaStream_t stream);
+void launch_eval(const double* ar, const CoreSlot* S, int d, const int* idx, int64_t M,
+                 double* out, int rcap, int* bad, int grid, cudaStream_t stream);
+void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int d,
+                  double* scratch, int64_t env_cap, double* out, cudaStream_t stream);
+cudaError_t eval_smem_optin(int rcap);
+
+}  // namespace ttg

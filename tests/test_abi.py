@@ -1,0 +1,70 @@
+"""The C-ABI library loads and exports every entry point include/*.h declares.
+
+Runs without a GPU: only symbol lookup, status strings and argument checks
+that return before any device work.
+"""
+import ctypes as C
+import glob
+import os
+import re
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b(ttg_\w+)\s*\(", src):
+            names.add(m.group(1))
+    return sorted(names)
+
+
+def test_header_declares_entry_points():
+    names = declared_functions()
+    for must in ("ttg_round", "ttg_round_batch", "ttg_matvec_round", "ttg_matmat_round",
+                 "ttg_eval_batch", "ttg_inner", "ttg_norm", "ttg_free",
+                 "ttg_right_orthogonalize"):
+        assert must in names
+
+
+def test_library_exports_every_declared_symbol(ttg):
+    lib = C.CDLL(ttg.library_path())
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+
+
+def test_status_strings_and_free(ttg):
+    L = ttg.lib()
+    assert L.ttg_status_string(0) == b"ok"
+    assert L.ttg_status_string(4) == b"index out of range"
+    t = ttg._Tensor()
+    L.ttg_free(C.byref(t))  # not owned: no-op
+
+
+def test_rejects_streaming_method_for_round(ttg):
+    # round_assert_method_for_value (round/round.hpp:124-134) -- checked
+    # before any device work, so this runs on a CPU-only host too.
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.round([__import__("numpy").ones((1, 2, 1))],
+                  ttg.RoundOptions(method=ttg.round_method.svd_streaming))
+    assert e.value.status == 3
+
+
+def test_no_silent_cpu_fallback(ttg):
+    """Without a usable device every compute entry point fails with
+    TTG_ERR_CUDA instead of computing on the host."""
+    try:
+        import torch
+        has_gpu = torch.cuda.is_available()
+    except Exception:
+        has_gpu = False
+    if has_gpu:
+        pytest.skip("a GPU is present")
+    import numpy as np
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.round([np.ones((1, 2, 2)), np.ones((2, 2, 1))], ttg.RoundOptions(eps=1e-8))
+    assert e.value.status == 9

@@ -1,0 +1,219 @@
+"""GPU parity: the CUDA path (through the C-ABI) against the CPU oracle.
+
+Tolerances: ranks must match the oracle exactly on these cases (no singular
+value sits in the delta tie region); tensors agree to a relative Frobenius
+error of 1e-11 (both sides are FP64; the QR/SVD algorithms differ only in
+operation order).  The reference tests each case restates are cited.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-11
+
+
+def _close(y, yref, tol=TOL):
+    assert O.ranks(y) == O.ranks(yref), (O.ranks(y), O.ranks(yref))
+    err = O.rel_err(y, yref)
+    assert err <= tol, err
+
+
+def cfg1():
+    a = O.random([4] * 10, 8, 42, fan_in_scale=True)
+    b = O.random([4] * 10, 8, 43, fan_in_scale=True)
+    return O.add(a, b)
+
+
+def test_round_config1(ttg):
+    t = cfg1()
+    info = ttg.RoundResult()
+    y = ttg.round(t, ttg.RoundOptions(eps=1e-8), info)
+    _close(y, O.round(t, 1e-8))
+    assert info.iters_run == 1 and info.converged and info.final_resid == 0.0
+    assert O.rel_err(y, t) <= 1e-8
+
+
+def test_round_right_canonical(ttg):
+    t = cfg1()
+    y = ttg.round(t, ttg.RoundOptions(eps=1e-8, gauge=ttg.round_gauge.right_canonical))
+    _close(y, O.round(t, 1e-8, gauge="right_canonical"))
+    # cores 1..d-1 right-orthogonal (round/tt_round.hpp:140-150)
+    for c in y[1:]:
+        M = c.reshape(c.shape[0], -1)
+        assert np.linalg.norm(M @ M.T - np.eye(M.shape[0])) <= 1e-13 * M.shape[0]
+
+
+def _inflate(cores, pad):
+    d = len(cores)
+    out = []
+    for k, c in enumerate(cores):
+        rl = 1 if k == 0 else c.shape[0] + pad
+        rr = 1 if k == d - 1 else c.shape[2] + pad
+        z = np.zeros((rl, c.shape[1], rr))
+        z[:c.shape[0], :, :c.shape[2]] = c
+        out.append(z)
+    return out
+
+
+def test_round_recovers_inflated(ttg):
+    # tests/core/test_tt_round.cpp:80-115 (zero-padded inflation; cap 2).
+    a = O.random([4, 5, 6, 4], 6, 13)
+    b = _inflate(a, 5)
+    y = ttg.round(b, ttg.RoundOptions(eps=1e-10))
+    assert O.rel_err(y, a) <= 1e-8
+    for k, r in enumerate(O.ranks(y)):
+        assert r <= O.ranks(a)[k]
+    _close(y, O.round(b, 1e-10))
+    ycap = ttg.round(b, ttg.RoundOptions(eps=1e-10, max_rank=2))
+    assert max(O.ranks(ycap)[1:-1]) <= 2
+    _close(ycap, O.round(b, 1e-10, max_rank=2))
+
+
+def test_round_zeros_and_d1(ttg):
+    # tests/core/test_tt_invariants.cpp:72-111.
+    z = O.zeros([3, 4, 2])
+    y = ttg.round(z, ttg.RoundOptions(eps=1e-10))
+    assert O.ranks(y) == [1, 1, 1, 1]
+    assert all(np.all(c == 0) for c in y)
+    one = O.ones([7])
+    y1 = ttg.round(one, ttg.RoundOptions(eps=1e-10))
+    assert np.max(np.abs(O.to_dense(y1) - O.to_dense(one))) < 1e-15
+
+
+def test_round_gauge_and_invariants(ttg):
+    # tests/core/test_tt_invariants.cpp:145-273.
+    r = ttg.round(O.random([3, 4, 5, 3], 6, 42), ttg.RoundOptions(eps=1e-10))
+    for c in r[:-1]:
+        M = c.reshape(-1, c.shape[2])
+        assert np.linalg.norm(M.T @ M - np.eye(M.shape[1])) <= 1e-14 * M.shape[1] * 10
+    a = O.random([2, 3, 4, 2], 8, 7)
+    n1 = O.norm(a)
+    assert O.norm(ttg.round(a, ttg.RoundOptions(eps=1e-2))) <= n1 * (1 + 1e-14)
+    assert O.norm(ttg.round(a, ttg.RoundOptions(max_rank=3))) <= n1 * (1 + 1e-14)
+    a = O.random([2, 3, 4, 2, 3], 6, 123)
+    r1 = ttg.round(a, ttg.RoundOptions(eps=1e-6))
+    r2 = ttg.round(r1, ttg.RoundOptions(eps=1e-6))
+    d1, d2 = O.to_dense(r1), O.to_dense(r2)
+    assert np.max(np.abs(d1 - d2)) <= 1e-14 * (np.linalg.norm(d1) + 1) * 10
+    a = O.random([2, 3, 4, 2], 8, 99)
+    ar = ttg.round(a, ttg.RoundOptions(eps=0.01))
+    assert O.norm(O.sub(a, ar)) <= 0.01 * O.norm(a) * 1.01
+
+
+def test_round_add_axpby_dense(ttg):
+    a = O.random([2, 3, 4], 4, 0)
+    b = O.random([2, 3, 4], 4, 1)
+    s = ttg.round(O.add(a, b), ttg.RoundOptions(eps=1e-10))
+    assert np.max(np.abs(O.to_dense(s) - (O.to_dense(a) + O.to_dense(b)))) < 1e-13
+    a = O.random([2, 3, 2], 4, 0)
+    b = O.random([2, 3, 2], 4, 1)
+    s = ttg.round(O.axpby(2.5, a, -0.7, b), ttg.RoundOptions(eps=1e-10))
+    ref = 2.5 * O.to_dense(a) - 0.7 * O.to_dense(b)
+    assert np.max(np.abs(O.to_dense(s) - ref)) < 1e-13
+
+
+def test_round_stress_cap(ttg):
+    # tests/core/test_tt_stress.cpp:49-124 (rank-12 {8,8,8,8}, cap 64, eps 1e-8)
+    a = O.random([8, 8, 8, 8], 12, 5)
+    b = O.random([8, 8, 8, 8], 12, 6)
+    t = O.add(a, b)
+    y = ttg.round(t, ttg.RoundOptions(eps=1e-8, max_rank=32))
+    _close(y, O.round(t, 1e-8, max_rank=32))
+
+
+def test_right_orthogonalize(ttg):
+    a = O.random([3, 4, 5, 3], 6, 99)
+    y = ttg.right_orthogonalize(a)
+    for c in y[1:]:
+        M = c.reshape(c.shape[0], -1)
+        assert np.linalg.norm(M @ M.T - np.eye(M.shape[0])) <= 1e-14 * M.shape[0] * 10
+    assert abs(O.norm(y) - O.norm(a)) <= 1e-14 * (O.norm(a) + 1) * 10
+    assert O.rel_err(y, a) <= 1e-13
+
+
+def test_round_batch_uneven(ttg):
+    tts = [O.random_uneven(1000 + i, 8, 16, 4, 24) for i in range(24)]
+    results = []
+    ys = ttg.round_batch(tts, ttg.RoundOptions(eps=1e-8), results)
+    for t, y, r in zip(tts, ys, results):
+        _close(y, O.round(t, 1e-8))
+        assert r.status == 0
+
+
+def test_matvec_round_naive_and_streaming(ttg):
+    # tests/core/test_tt_matrix_apply_round.cpp:31-129.
+    A = O.random_matrix([2, 3, 2, 3], [3, 2, 3, 2], 3, 0xAA11)
+    x = O.random([3, 2, 3, 2], 3, 0xBB22)
+    yn = ttg.matvec_round(A, x, ttg.RoundOptions(eps=1e-10))
+    _close(yn, O.matvec_round(A, x, 1e-10))
+    ys = ttg.matvec_round(A, x, ttg.RoundOptions(eps=1e-10,
+                                                   method=ttg.round_method.svd_streaming))
+    _close(ys, O.matvec_round(A, x, 1e-10, method="svd_streaming"))
+    yd, sd = O.to_dense(yn), O.to_dense(ys)
+    assert np.linalg.norm(yd - sd) <= 10 * 1e-10 * np.linalg.norm(yd)
+    ym = ttg.matvec(A, x)
+    _close(ym, O.matvec(A, x), 1e-13)
+    cap = ttg.matvec_round(O.random_matrix([2, 3, 2, 2], [3, 2, 3, 2], 3, 0xE5E5E5),
+                           O.random([3, 2, 3, 2], 3, 0xF6F6F6),
+                           ttg.RoundOptions(eps=1e-12, max_rank=2))
+    assert max(O.ranks(cap)) <= 2
+
+
+def test_matmat_round(ttg):
+    A = O.random_matrix([2, 3, 2, 3], [3, 2, 3, 2], 2, 0xCC33)
+    B = O.random_matrix([3, 2, 3, 2], [2, 3, 2, 3], 2, 0xDD44)
+    cs = ttg.matmat_round(A, B, ttg.RoundOptions(eps=1e-10))
+    _close(cs, O.matmat_round(A, B, 1e-10))
+    cn = ttg.matmat_round(A, B, ttg.RoundOptions(eps=1e-10, method=ttg.round_method.svd_naive))
+    _close(cn, O.matmat_round(A, B, 1e-10, method="svd_naive"))
+    assert cs[0].ndim == 4
+    cm = ttg.matmat(A, B)
+    _close(cm, O.matmat(A, B), 1e-13)
+
+
+def test_matvec_round_config2_small(ttg):
+    # Config-2 shapes at reduced d: MPO rank 8 x TT rank 32, n = m = 4.
+    A = O.random_matrix([4] * 6, [4] * 6, 8, 44, fan_in_scale=True)
+    x = O.random([4] * 6, 32, 45, fan_in_scale=True)
+    for method in ("svd", "svd_streaming"):
+        y = ttg.matvec_round(A, x, ttg.RoundOptions(eps=1e-10, method=ttg.round_method[method]))
+        _close(y, O.matvec_round(A, x, 1e-10, method=method), 1e-10)
+
+
+def test_eval_inner_norm(ttg):
+    a = O.random([4, 5, 6, 4], 6, 13)
+    rng = np.random.default_rng(3)
+    idx = np.stack([rng.integers(0, n, 500) for n in (4, 5, 6, 4)], axis=1).astype(np.int32)
+    v = ttg.eval_batch(a, idx)
+    dense = O.to_dense(a).reshape(4, 5, 6, 4)
+    ref = dense[idx[:, 0], idx[:, 1], idx[:, 2], idx[:, 3]]
+    assert np.max(np.abs(v - ref)) <= 1e-12
+    b = O.random([4, 5, 6, 4], 5, 14)
+    assert abs(ttg.inner(a, b) - O.inner(a, b)) <= 1e-12 * (abs(O.inner(a, b)) + 1)
+    assert abs(ttg.norm(a) - O.norm(a)) <= 1e-12 * O.norm(a)
+    assert ttg.inner(O.zeros([3, 4, 2]), O.zeros([3, 4, 2])) == 0.0
+
+
+def test_errors(ttg):
+    t = cfg1()
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.round(t, ttg.RoundOptions(method=ttg.round_method.svd_streaming))
+    assert e.value.status == 3
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.inner(O.random([2, 3], 2, 0), O.random([2, 4], 2, 0))
+    assert e.value.status == 2
+    a = O.random([4, 4], 2, 1)
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.eval_batch(a, np.array([[0, 4]], np.int32))
+    assert e.value.status == 4
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.eval_batch([], np.zeros((1, 0), np.int32))
+    assert e.value.status == 10
+    A = O.random_matrix([2, 2], [2, 2], 2, 1)
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.matvec_round(A, O.random([2, 2], 2, 2),
+                         ttg.RoundOptions(method=ttg.round_method.svd_naive))
+    assert e.value.status == 3
