@@ -1,0 +1,311 @@
+#!/usr/bin/env python
+"""Throughput of the TT-rounding hot path on GB300.
+
+Default workload (the headline): batched uneven rounding -- 4096 independent
+TTs, TT i seeded with mt19937_64(1000 + i): d ~ U[8,32], n_k ~ {2,4,8}, bond
+ranks ~ U[4,96] (feasibility-clipped), entries N(0,1)/sqrt(r_k n_k),
+eps = 1e-8, plain FP64, one persistent launch per step.  A step is one
+round(const tt&) of every TT: the deep copy of the inputs into the work
+arena (round/tt_round.hpp:129-134) plus the sweep kernel.
+
+Prints one JSON line (rank 0).  `--impl reference` times the reference's CPU
+algorithm (the oracle port: the reference itself needs Eigen, which is absent)
+on the host cores instead.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import time
+from concurrent.futures import ThreadPoolExecutor
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+METRIC = ("TT roundings/sec and matvec_round/sec at rel. err<=1e-8: mixed/learned vs plain "
+          "FP64, 1 GB300")
+EPS = 1e-8
+SEED0 = 1000
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    ap.add_argument("--count", type=int, default=4096)
+    ap.add_argument("--e2e-steps", type=int, default=2)
+    ap.add_argument("--cpu-sample", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def workload_config(count):
+    return {
+        "workload": (f"batched uneven rounding: {count} TTs, d~U[8,32], n_k~{{2,4,8}}, "
+                     "bond ranks~U[4,96] clipped, N(0,1)/sqrt(r n) cores, eps=1e-8, "
+                     "round(const tt&) per TT"),
+        "count": count, "eps": EPS, "precision": "fp64", "seeds": f"{SEED0}+i",
+        "l2": "inputs (~4.5 GB FP64) exceed L2 (129 MB); no flush needed",
+    }
+
+
+def make_batch(T, count, base):
+    with ThreadPoolExecutor(max_workers=min(32, os.cpu_count() or 4)) as ex:
+        return list(ex.map(lambda i: T.random_uneven(base + i), range(count)))
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        self.lines = []
+        if self.proc:
+            self.proc.terminate()
+            try:
+                out, _ = self.proc.communicate(timeout=5)
+            except Exception:
+                self.proc.kill()
+                out = ""
+            self.lines = [ln for ln in out.splitlines() if ln.strip()]
+
+    def summary(self):
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in getattr(self, "lines", []):
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def dist_setup(gpus):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return rank, world, local
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    import tensor_train_gb300 as T
+    from tensor_train_gb300.flops import round_flops
+
+    rank, world, local = dist_setup(args.gpus)
+    torch.cuda.set_device(local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl", device_id=torch.device("cuda", local))
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+
+    count = args.count
+    base = SEED0 + rank * count  # weak scaling: each rank owns its own batch
+    tts = make_batch(T, count, base)
+    opts = T.RoundOptions(eps=EPS)
+    plan = T.Plan("round", tts, opts=opts)
+    plan.upload(sptr)
+    torch.cuda.synchronize()
+
+    def barrier():
+        if world > 1:
+            torch.distributed.barrier()
+
+    for _ in range(args.warmup):
+        plan.run(sptr)
+    torch.cuda.synchronize()
+    outs = plan.download(sptr)
+    bad = [r.status for r in plan.results if r.status not in (0,)]
+
+    launches0 = T.kernel_launches()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    barrier()
+    torch.cuda.synchronize()
+    with Clocks(local) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.run(sptr)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = T.kernel_launches() - launches0
+    ms_total = ev0.elapsed_time(ev1)
+    if world > 1:
+        t = torch.tensor([ms_total], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms_total = float(t.item())
+    ms_step = ms_total / args.steps
+    value = count * world / (ms_step / 1e3)
+
+    # Kernel-only time of the sweep launch (roofline).
+    kms = []
+    for _ in range(3):
+        plan.run(sptr)
+        kms.append(plan.kernel_ms())
+    kernel_ms = statistics.mean(kms)
+    flops = 0.0
+    for t_in, t_out in zip(tts, outs):
+        modes = [c.shape[1] for c in t_in]
+        rin = [t_in[0].shape[0]] + [c.shape[-1] for c in t_in]
+        rout = [t_out[0].shape[0]] + [c.shape[-1] for c in t_out]
+        flops += round_flops(modes, rin, rout)
+    peak = T.device_fp64_peak()
+    achieved = flops / (kernel_ms / 1e3) / 1e12
+
+    # End to end through the C-ABI with host buffers: pack + H2D + sweep +
+    # D2H + unpack inside ttg_round_batch.  Inputs marshalled beforehand.
+    import ctypes as C
+    srcs = [T._In(t) for t in tts]
+    ins = (T._Tensor * count)(*[s.t for s in srcs])
+    copts = T._opts(opts)
+    h2d, d2h = plan.io_bytes()
+    e2e_ms = []
+    for i in range(args.e2e_steps + 1):
+        outs_c = (T._Tensor * count)()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        st = T.lib().ttg_round_batch(count, ins, C.byref(copts), outs_c, None)
+        t1 = time.perf_counter()
+        for j in range(count):
+            T.lib().ttg_free(C.byref(outs_c[j]))
+        assert st == 0, T.lib().ttg_last_error()
+        if i > 0:  # first call is the warm-up (pool growth)
+            e2e_ms.append((t1 - t0) * 1e3)
+    e2e_step = statistics.mean(e2e_ms)
+    e2e_value = count * world / (e2e_step / 1e3)
+    if world > 1:
+        t = torch.tensor([e2e_step], device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_value = count * world / (float(t.item()) / 1e3)
+
+    line = {
+        "metric": METRIC, "value": value, "unit": "roundings/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded uneven random TTs (mt19937_64 + normal_distribution)",
+        "config": dict(workload_config(count), parallelism=f"{world} independent shard(s)"),
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "traffic": None,
+                     "kernel": "round_kernel", "kernel_ms": kernel_ms,
+                     "flops_per_launch": flops,
+                     "peak_source": "measured FP64 FMA loop on this GPU (ttg_device_fp64_peak)"},
+        "e2e": {"value": e2e_value, "unit": "roundings/s", "h2d_bytes_per_step": h2d,
+                "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
+        "gpu_launches": launches,
+        "clocks": clk.summary(),
+        "device_status_errors": len(bad),
+    }
+
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(tts, outs, args.cpu_sample)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        torch.distributed.destroy_process_group()
+
+
+def cpu_baseline(tts, gpu_outs, sample):
+    """The oracle (FP64 port of the reference's round) on the host cores, on
+    a strided sample of the same batch; also checks the GPU outputs of the
+    sampled TTs against it (ranks and relative Frobenius error)."""
+    from oracle import pyoracle as O
+    stride = max(1, len(tts) // sample)
+    idx = list(range(0, len(tts), stride))[:sample]
+    threads = os.cpu_count() or 1
+    sec, ref = O.round_many_timed([tts[i] for i in idx], EPS, 0, threads)
+    errs, ranks_ok = [], True
+    for j, i in enumerate(idx[:16]):
+        y = gpu_outs[i]
+        yr = ref[j].cores()
+        ranks_ok &= O.ranks(y) == O.ranks(yr)
+        errs.append(O.rel_err(y, yr))
+    return {"value": len(idx) / sec, "unit": "roundings/s", "cores": threads, "kind": "port",
+            "sample": f"{len(idx)} of the {len(tts)} TTs (every {stride}th), oracle FP64 "
+                      f"round on {threads} host threads, {sec:.2f} s",
+            "parity_checked": len(errs), "max_rel_err_vs_oracle": max(errs),
+            "ranks_equal": bool(ranks_ok)}
+
+
+def run_reference(args):
+    """CPU implementation of the path (oracle port: the reference needs
+    Eigen, which is absent) on all host threads, same workload."""
+    rank, world, _ = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    import tensor_train_gb300 as T
+    from oracle import pyoracle as O
+    threads = os.cpu_count() or 1
+    per_step = max(threads * 4, 64)
+    need = per_step * (args.steps + args.warmup)
+    stride = max(1, args.count // need)
+    tts = make_batch(T, need, SEED0) if stride == 1 else \
+        [T.random_uneven(SEED0 + i * stride) for i in range(need)]
+    times = []
+    for s in range(args.warmup + args.steps):
+        chunk = tts[s * per_step:(s + 1) * per_step]
+        sec, _ = O.round_many_timed(chunk, EPS, 0, threads)
+        if s >= args.warmup:
+            times.append(sec)
+    step = statistics.mean(times)
+    value = per_step / step
+    line = {
+        "metric": METRIC, "value": value, "unit": "roundings/s", "n_gpus": args.gpus,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": step * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic: seeded uneven random TTs (mt19937_64 + normal_distribution)",
+        "config": workload_config(args.count), "impl": "reference",
+        "cpu_baseline": {"value": value, "unit": "roundings/s", "cores": threads, "kind": "port",
+                         "sample": f"{per_step} TTs of the batch per step on {threads} threads"},
+        "e2e": {"value": value, "unit": "roundings/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -161,6 +161,34 @@ int32_t ttg_eval_batch(const ttg_tensor* a, const int32_t* idx, int32_t M, doubl
 int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out);
 int32_t ttg_norm(const ttg_tensor* a, double* out);
 
+/* ---- host-side input construction (no device work) --------------------
+ * Replaces: tt random(const std::vector<int>& shape, int max_rank,
+ *           std::uint64_t seed) (factory/tt_factory.hpp:141-207) when
+ *           cols == NULL, and tt_matrix random(row_shape, col_shape, max_rank,
+ *           seed) (factory/tt_matrix_factory.hpp:133-191) otherwise.  With
+ *           fan_in_scale != 0 each core is multiplied by 1/sqrt(r_k*mode_k)
+ *           after drawing. */
+int32_t ttg_host_random(int32_t d, const int32_t* rows, const int32_t* cols, int32_t max_rank,
+                        uint64_t seed, int32_t fan_in_scale, ttg_tensor* out);
+/* The uneven batch member: mt19937_64(seed) draws d ~ U{dmin..dmax},
+ * n_k ~ U{2,4,8}, bond ranks ~ U{rmin..rmax}, clips them for feasibility,
+ * then fills N(0,1)/sqrt(r_k*n_k) entries from the same stream.  No
+ * reference counterpart (the reference has no batched workload). */
+int32_t ttg_host_random_uneven(uint64_t seed, int32_t dmin, int32_t dmax, int32_t rmin,
+                               int32_t rmax, ttg_tensor* out);
+/* Replaces: tt ones(const std::vector<int>&) (factory/tt_factory.hpp:60-78). */
+int32_t ttg_host_ones(int32_t d, const int32_t* shape, ttg_tensor* out);
+/* Replaces: tt axpby(double, const tt&, double, const tt&)
+ *           (algebra/tt_ops.hpp:72-117); add = axpby(1,a,1,b), sub = axpby(1,a,-1,b). */
+int32_t ttg_host_axpby(double alpha, const ttg_tensor* a, double beta, const ttg_tensor* b,
+                       ttg_tensor* out);
+const char* ttg_host_last_error(void);
+
+/* Measured FP64 FMA throughput of the current device (TFLOP/s): a
+ * dependent-chain DFMA loop over all SMs, timed with CUDA events.  Used as
+ * the roofline denominator of the FP64 kernels.  No reference counterpart. */
+int32_t ttg_device_fp64_peak(double* tflops);
+
 /* ---- device-resident plans (inputs already in HBM) --------------------
  * A plan owns a device arena holding a set of tensors; run() executes the
  * sweep on `stream` (a cudaStream_t, NULL = legacy default) without host
@@ -173,14 +201,21 @@ int32_t ttg_plan_create_round(int32_t count, const ttg_tensor* ins, const ttg_ro
 int32_t ttg_plan_create_matvec_round(const ttg_tensor* A, const ttg_tensor* x,
                                      const ttg_round_options* opts, ttg_plan** plan);
 int32_t ttg_plan_create_eval(const ttg_tensor* a, const int32_t* idx, int32_t M, ttg_plan** plan);
-/* Re-uploads the inputs given at creation (host -> device) on `stream`. */
+/* Re-uploads the inputs given at creation (host -> device) on `stream` into
+ * the plan's input arena. */
 int32_t ttg_plan_upload(ttg_plan* plan, void* stream);
+/* One pass of the hot path: copies the input arena into the work arena
+ * (the deep copy of round(const tt&), round/tt_round.hpp:129-134) and runs
+ * the sweep on it.  Idempotent: repeated runs give the same result. */
 int32_t ttg_plan_run(ttg_plan* plan, void* stream);
 /* Copies results back (device -> host) and synchronises `stream`.
  * For round plans `outs` receives `count` tensors; for eval plans
  * `values` receives M doubles. */
 int32_t ttg_plan_download(ttg_plan* plan, void* stream, ttg_tensor* outs, double* values,
                           ttg_round_result* results);
+/* Device time (ms) of the sweep kernel of the last run(), from events
+ * recorded on the run's stream around that launch alone. */
+int32_t ttg_plan_kernel_ms(ttg_plan* plan, float* ms);
 /* Bytes moved host->device by upload and device->host by download. */
 int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);
 void ttg_plan_destroy(ttg_plan* plan);

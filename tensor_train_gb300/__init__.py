@@ -30,6 +30,8 @@ __all__ = [
     "RoundOptions", "RoundResult", "TTGError", "round_method", "round_gauge", "precision",
     "round", "round_batch", "matvec_round", "matmat_round", "matvec", "matmat", "eval_batch",
     "inner", "norm", "right_orthogonalize", "Plan", "lib", "library_path", "kernel_launches",
+    "random", "random_matrix", "random_uneven", "ones", "axpby", "add", "sub",
+    "device_fp64_peak",
 ]
 
 
@@ -144,6 +146,15 @@ def lib():
         "ttg_plan_io_bytes": (C.c_int32, [C.c_void_p, C.POINTER(C.c_int64),
                                           C.POINTER(C.c_int64)]),
         "ttg_plan_destroy": (None, [C.c_void_p]),
+        "ttg_plan_kernel_ms": (C.c_int32, [C.c_void_p, C.POINTER(C.c_float)]),
+        "ttg_host_random": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                        C.c_int32, C.c_uint64, C.c_int32, T]),
+        "ttg_host_random_uneven": (C.c_int32, [C.c_uint64, C.c_int32, C.c_int32, C.c_int32,
+                                               C.c_int32, T]),
+        "ttg_host_ones": (C.c_int32, [C.c_int32, C.POINTER(C.c_int32), T]),
+        "ttg_host_axpby": (C.c_int32, [C.c_double, T, C.c_double, T, T]),
+        "ttg_host_last_error": (C.c_char_p, []),
+        "ttg_device_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -399,6 +410,11 @@ class Plan:
         self.results = [_result(res[i]) for i in range(self.count)]
         return cores
 
+    def kernel_ms(self) -> float:
+        v = C.c_float()
+        _check(lib().ttg_plan_kernel_ms(self.h, C.byref(v)), "plan_kernel_ms")
+        return v.value
+
     def io_bytes(self):
         a, b = C.c_int64(), C.c_int64()
         _check(lib().ttg_plan_io_bytes(self.h, C.byref(a), C.byref(b)), "plan_io_bytes")
@@ -414,3 +430,71 @@ class Plan:
             self.close()
         except Exception:
             pass
+
+
+# -- host-side input construction (factory/tt_factory.hpp, algebra/tt_ops.hpp) --
+def _host_check(st, what):
+    if st != 0:
+        raise TTGError(st, f"{what}: {lib().ttg_host_last_error().decode()}")
+
+
+def random(shape, max_rank, seed, fan_in_scale=False):
+    """random(shape, max_rank, seed) (factory/tt_factory.hpp:141-207)."""
+    sh = np.ascontiguousarray(shape, np.int32)
+    out = _Tensor()
+    _host_check(lib().ttg_host_random(len(sh), sh.ctypes.data_as(C.POINTER(C.c_int32)),
+                                      C.POINTER(C.c_int32)(), int(max_rank), int(seed),
+                                      int(bool(fan_in_scale)), C.byref(out)), "random")
+    return _take(out)
+
+
+def random_matrix(rows, cols, max_rank, seed, fan_in_scale=False):
+    """random(row_shape, col_shape, max_rank, seed) (factory/tt_matrix_factory.hpp:133-191)."""
+    r = np.ascontiguousarray(rows, np.int32)
+    c = np.ascontiguousarray(cols, np.int32)
+    out = _Tensor()
+    _host_check(lib().ttg_host_random(len(r), r.ctypes.data_as(C.POINTER(C.c_int32)),
+                                      c.ctypes.data_as(C.POINTER(C.c_int32)), int(max_rank),
+                                      int(seed), int(bool(fan_in_scale)), C.byref(out)),
+                "random_matrix")
+    return _take(out)
+
+
+def random_uneven(seed, dmin=8, dmax=32, rmin=4, rmax=96):
+    """One member of the uneven batch (seeded d, n_k, ranks and entries)."""
+    out = _Tensor()
+    _host_check(lib().ttg_host_random_uneven(int(seed), dmin, dmax, rmin, rmax, C.byref(out)),
+                "random_uneven")
+    return _take(out)
+
+
+def ones(shape):
+    sh = np.ascontiguousarray(shape, np.int32)
+    out = _Tensor()
+    _host_check(lib().ttg_host_ones(len(sh), sh.ctypes.data_as(C.POINTER(C.c_int32)),
+                                    C.byref(out)), "ones")
+    return _take(out)
+
+
+def axpby(alpha, a, beta, b):
+    """axpby (algebra/tt_ops.hpp:72-117)."""
+    sa, sb = _In(a), _In(b)
+    out = _Tensor()
+    _host_check(lib().ttg_host_axpby(float(alpha), C.byref(sa.t), float(beta), C.byref(sb.t),
+                                     C.byref(out)), "axpby")
+    return _take(out)
+
+
+def add(a, b):
+    return axpby(1.0, a, 1.0, b)
+
+
+def sub(a, b):
+    return axpby(1.0, a, -1.0, b)
+
+
+def device_fp64_peak() -> float:
+    """Measured FP64 FMA throughput of the current device in TFLOP/s."""
+    v = C.c_double()
+    _check(lib().ttg_device_fp64_peak(C.byref(v)), "device_fp64_peak")
+    return v.value

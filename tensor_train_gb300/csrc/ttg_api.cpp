@@ -227,7 +227,8 @@ struct ttg_plan
   std::vector<Apply> applies;
   // byte layout of the device buffer
   size_t off_arena = 0, off_slots = 0, off_tts = 0, off_order = 0, off_aidx = 0, off_bidx = 0,
-         off_oidx = 0, prefix_bytes = 0, off_queue = 0, off_scratch = 0, total_bytes = 0;
+         off_oidx = 0, prefix_bytes = 0, off_pristine = 0, off_queue = 0, off_scratch = 0,
+         total_bytes = 0;
   DevMem dev;
   HostPinned host;
   // eval plans
@@ -236,13 +237,13 @@ struct ttg_plan
   int rcap = 0;
   size_t off_idx = 0, off_out = 0, off_bad = 0;
   int64_t h2d = 0, d2h = 0;
-  cudaEvent_t ev0 = nullptr, ev1 = nullptr;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
+  bool kernel_timed = false;
   ~ttg_plan()
   {
-    if (ev0)
-      cudaEventDestroy(ev0);
-    if (ev1)
-      cudaEventDestroy(ev1);
+    for (cudaEvent_t e : {ev0, ev1, evk0, evk1})
+      if (e)
+        cudaEventDestroy(e);
   }
 };
 
@@ -350,6 +351,8 @@ int32_t layout_and_alloc(ttg_plan& P)
   P.off_oidx = o;
   o = align256(o + sizeof(int32_t) * P.out_idx.size());
   P.prefix_bytes = o;
+  P.off_pristine = o;
+  o = align256(o + P.prefix_bytes);
   P.off_queue = o;
   o = align256(o + 256);
   P.off_scratch = o;
@@ -359,6 +362,8 @@ int32_t layout_and_alloc(ttg_plan& P)
   TTG_CUDA(P.host.ensure(P.prefix_bytes));
   TTG_CUDA(cudaEventCreate(&P.ev0));
   TTG_CUDA(cudaEventCreate(&P.ev1));
+  TTG_CUDA(cudaEventCreate(&P.evk0));
+  TTG_CUDA(cudaEventCreate(&P.evk1));
   // Host image of the prefix: arena inputs + tables.
   char* h = static_cast<char*>(P.host.p);
   std::memset(h, 0, P.prefix_bytes);
@@ -466,9 +471,13 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
   return layout_and_alloc(P);
 }
 
+// Inputs land in the pristine copy; run() deep-copies them into the work
+// region, so a plan can be run any number of times.
 int32_t plan_upload(ttg_plan& P, cudaStream_t st)
 {
-  TTG_CUDA(cudaMemcpyAsync(P.dev.p, P.host.p, P.prefix_bytes, cudaMemcpyHostToDevice, st));
+  char* d = static_cast<char*>(P.dev.p);
+  TTG_CUDA(cudaMemcpyAsync(d + P.off_pristine, P.host.p, P.prefix_bytes, cudaMemcpyHostToDevice,
+                           st));
   return TTG_OK;
 }
 
@@ -491,6 +500,7 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
     TTG_CUDA(cudaGetLastError());
     return TTG_OK;
   }
+  TTG_CUDA(cudaMemcpyAsync(d, d + P.off_pristine, P.prefix_bytes, cudaMemcpyDeviceToDevice, st));
   double* arena = reinterpret_cast<double*>(d + P.off_arena);
   for (const auto& a : P.applies)
   {
@@ -501,7 +511,10 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
   if (!P.order.empty() && P.job_kind >= 0)
   {
     TTG_CUDA(cudaMemsetAsync(d + P.off_queue, 0, sizeof(int32_t), st));
+    TTG_CUDA(cudaEventRecord(P.evk0, st));
     launch_round(make_job(P), P.grid, st);
+    TTG_CUDA(cudaEventRecord(P.evk1, st));
+    P.kernel_timed = true;
     g_launches += 1;
   }
   TTG_CUDA(cudaGetLastError());
@@ -595,6 +608,30 @@ cudaStream_t lib_stream()
 }
 
 std::mutex g_mu;
+
+// Buffers reused by the one-shot entry points (grow-only, guarded by g_mu),
+// so repeated calls do not pay cudaMalloc / cudaHostAlloc again.
+DevMem g_dev_pool;
+HostPinned g_host_pool;
+
+struct PoolLease
+{
+  ttg_plan& P;
+  explicit PoolLease(ttg_plan& p) : P(p)
+  {
+    std::swap(P.dev.p, g_dev_pool.p);
+    std::swap(P.dev.bytes, g_dev_pool.bytes);
+    std::swap(P.host.p, g_host_pool.p);
+    std::swap(P.host.bytes, g_host_pool.bytes);
+  }
+  ~PoolLease()
+  {
+    std::swap(P.dev.p, g_dev_pool.p);
+    std::swap(P.dev.bytes, g_dev_pool.bytes);
+    std::swap(P.host.p, g_host_pool.p);
+    std::swap(P.host.bytes, g_host_pool.bytes);
+  }
+};
 
 // Runs a plan end to end on the library stream with device timing.
 int32_t execute(ttg_plan& P, float* ms)
@@ -721,6 +758,17 @@ int32_t ttg_plan_run(ttg_plan* P, void* stream)
   return plan_run(*P, static_cast<cudaStream_t>(stream));
 }
 
+int32_t ttg_plan_kernel_ms(ttg_plan* P, float* ms)
+{
+  if (!P || !ms)
+    return fail(TTG_ERR_ARG, "plan_kernel_ms: null argument");
+  if (!P->kernel_timed)
+    return fail(TTG_ERR_ARG, "plan_kernel_ms: no sweep launch recorded");
+  TTG_CUDA(cudaEventSynchronize(P->evk1));
+  TTG_CUDA(cudaEventElapsedTime(ms, P->evk0, P->evk1));
+  return TTG_OK;
+}
+
 int32_t ttg_plan_io_bytes(const ttg_plan* P, int64_t* h2d, int64_t* d2h)
 {
   if (!P)
@@ -794,6 +842,7 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
     return st;
   std::lock_guard<std::mutex> lk(g_mu);
   ttg_plan P;
+  PoolLease lease(P);
   if (int32_t st = build_round_plan(P, count, ins, opts, op))
     return st;
   float ms = 0.0f;
@@ -1011,6 +1060,7 @@ static int32_t apply_round_common(const ttg_tensor* a, const ttg_tensor* x,
   }
   std::lock_guard<std::mutex> lk(g_mu);
   ttg_plan P;
+  PoolLease lease(P);
   int32_t st = (mode == 2) ? build_stream_plan(P, A, X, opts)
                            : build_apply_plan(P, A, X, mode == 1, opts);
   if (st)
@@ -1262,6 +1312,7 @@ int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out)
   if (int32_t e = plan_upload(P, st))
     return e;
   char* d = static_cast<char*>(P.dev.p);
+  TTG_CUDA(cudaMemcpyAsync(d, d + P.off_pristine, P.prefix_bytes, cudaMemcpyDeviceToDevice, st));
   double* scratch = reinterpret_cast<double*>(d + P.off_scratch);
   const CoreSlot* S = reinterpret_cast<const CoreSlot*>(d + P.off_slots);
   launch_inner(reinterpret_cast<double*>(d + P.off_arena), S + P.tts[0].first,
@@ -1271,6 +1322,34 @@ int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out)
   TTG_CUDA(cudaMemcpyAsync(out, scratch + P.scratch_stride - 8, sizeof(double),
                            cudaMemcpyDeviceToHost, st));
   TTG_CUDA(cudaStreamSynchronize(st));
+  return TTG_OK;
+}
+
+int32_t ttg_device_fp64_peak(double* tflops)
+{
+  g_err.clear();
+  if (!tflops)
+    return fail(TTG_ERR_ARG, "fp64_peak: null output");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  const int grid = 4 * std::max(device().sms, 1), block = 256, iters = 1 << 14;
+  DevMem buf;
+  TTG_CUDA(buf.ensure(sizeof(double) * static_cast<size_t>(grid) * block));
+  cudaStream_t st = lib_stream();
+  cudaEvent_t e0, e1;
+  TTG_CUDA(cudaEventCreate(&e0));
+  TTG_CUDA(cudaEventCreate(&e1));
+  launch_fp64_peak(static_cast<double*>(buf.p), 64, grid, block, st);
+  TTG_CUDA(cudaEventRecord(e0, st));
+  launch_fp64_peak(static_cast<double*>(buf.p), iters, grid, block, st);
+  TTG_CUDA(cudaEventRecord(e1, st));
+  TTG_CUDA(cudaEventSynchronize(e1));
+  float ms = 0.0f;
+  TTG_CUDA(cudaEventElapsedTime(&ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *tflops = 2.0 * 8 * iters * static_cast<double>(grid) * block / (ms * 1e-3) / 1e12;
   return TTG_OK;
 }
 

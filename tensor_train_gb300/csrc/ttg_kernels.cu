@@ -846,6 +846,30 @@ void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int 
   inner_kernel<<<1, kThreads, 0, stream>>>(ar, SA, SB, d, scratch, env_cap, out);
 }
 
+// Eight independent DFMA chains per thread; one store per thread into
+// out[grid*block].
+__global__ void fp64_peak_kernel(double* out, int iters)
+{
+  double x[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    x[k] = threadIdx.x + k;
+  for (int i = 0; i < iters; ++i)
+#pragma unroll
+    for (int k = 0; k < 8; ++k)
+      x[k] = fma(x[k], 0.999, 0.001);
+  double s = 0.0;
+#pragma unroll
+  for (int k = 0; k < 8; ++k)
+    s += x[k];
+  out[static_cast<int64_t>(blockIdx.x) * blockDim.x + threadIdx.x] = s;
+}
+
+void launch_fp64_peak(double* out, int iters, int grid, int block, cudaStream_t stream)
+{
+  fp64_peak_kernel<<<grid, block, 0, stream>>>(out, iters);
+}
+
 cudaError_t eval_smem_optin(int rcap)
 {
   const size_t smem = static_cast<size_t>(kWarps) * 2 * rcap * sizeof(double);
