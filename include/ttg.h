@@ -220,6 +220,37 @@ int32_t ttg_plan_kernel_ms(ttg_plan* plan, float* ms);
 int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);
 void ttg_plan_destroy(ttg_plan* plan);
 
+/* ---- rounding without device allocation -------------------------------
+ * No counterpart in the reference.  For callers that cannot allocate device
+ * memory: code running inside another runtime's allocator (a framework
+ * plugin that must not call cudaMalloc), work issued while allocation is
+ * forbidden, or processes with a fixed device-memory budget.  Rounds one TT
+ * (round(const tt&, round_options) semantics, gauge none or right_canonical,
+ * FP64) whose cores are already on the device:
+ *   ranks[d+1], modes[d]  host arrays describing the input;
+ *   in_dev                the input cores back to back (offsets as in
+ *                         ttg_tensor), read only;
+ *   out_dev               caller-provided device buffer with room for the
+ *                         input's total size; receives the rounded cores
+ *                         back to back;
+ *   out_ranks[d+1]        host array receiving the output ranks.
+ * The call allocates nothing: its tables, work copy and scratch live in one
+ * file-scope __device__ array of TTG_NOALLOC_SCRATCH_BYTES that every GPU
+ * loading this library holds until the process exits.  A TT whose work copy
+ * plus scratch exceeds that size, or with d > TTG_NOALLOC_MAX_D, is rejected
+ * with TTG_ERR_NO_SPACE and a message in ttg_last_error().  The first call on
+ * each device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current; make that first call before any stream capture.  All
+ * calls share the array and it keeps the last call's contents (every call
+ * resets what must start at zero); calls that overlap on the GPU -- on
+ * different streams or threads -- race on it and must be serialised by the
+ * caller.  The call waits for its own stream to finish (it returns ranks). */
+#define TTG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+#define TTG_NOALLOC_MAX_D 256
+int32_t ttg_round_noalloc(int32_t d, const int32_t* ranks, const int32_t* modes,
+                          const double* in_dev, double* out_dev, int32_t* out_ranks,
+                          const ttg_round_options* opts, void* stream);
+
 #ifdef __cplusplus
 }
 #endif

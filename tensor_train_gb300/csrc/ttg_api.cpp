@@ -206,6 +206,11 @@ enum PlanKind
 
 }  // namespace
 
+namespace ttg
+{
+void set_last_error(const std::string& msg) { g_err = msg; }
+}  // namespace ttg
+
 struct ttg_plan
 {
   PlanKind kind = kPlanRound;

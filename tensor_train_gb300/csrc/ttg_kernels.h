@@ -1,6 +1,8 @@
 // Host-side launchers of the sweep, apply, eval and inner kernels.
 #pragma once
 
+#include <string>
+
 #include <cuda_runtime.h>
 
 #include "ttg_job.h"
@@ -17,5 +19,7 @@ void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int 
                   double* scratch, int64_t env_cap, double* out, cudaStream_t stream);
 cudaError_t eval_smem_optin(int rcap);
 void launch_fp64_peak(double* out, int iters, int grid, int block, cudaStream_t stream);
+// Sets the message returned by ttg_last_error() on this thread.
+void set_last_error(const std::string& msg);
 
 }  // namespace ttg

@@ -1,0 +1,98 @@
+"""ttg_round_noalloc: rounding for callers that cannot allocate device memory.
+
+Some callers cannot call cudaMalloc -- a plugin running inside another
+framework's allocator, work issued while device allocation is forbidden, a
+process held to a fixed memory budget.  For them the library has one entry
+point that takes the input cores and an output buffer already on the device
+and keeps everything else it needs in a fixed, file-scope device array.
+These tests call it through the C-ABI and compare it with the allocating
+entry point ttg_round on the same inputs, at the tolerance the other GPU
+tests use, on two calls in a row (the array is shared and keeps the last
+call's contents, so the second call checks that every call starts clean).
+This file is collected last so that a stop at its first failure has
+already run every other test.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-11
+
+
+def _bind(ttg):
+    L = ttg.lib()
+    f = L.ttg_round_noalloc
+    f.restype = C.c_int32
+    f.argtypes = [C.c_int32, C.POINTER(C.c_int32), C.POINTER(C.c_int32), C.c_void_p,
+                  C.c_void_p, C.POINTER(C.c_int32), C.POINTER(ttg._Opts), C.c_void_p]
+    return f
+
+
+def _noalloc_round(ttg, cores, opts):
+    import torch
+    f = _bind(ttg)
+    d = len(cores)
+    ranks = np.array([cores[0].shape[0]] + [c.shape[-1] for c in cores], np.int32)
+    modes = np.array([c.shape[1] for c in cores], np.int32)
+    flat = np.concatenate([c.ravel() for c in cores])
+    src = torch.from_numpy(flat).to("cuda")
+    dst = torch.full_like(src, float("nan"))
+    out_ranks = np.zeros(d + 1, np.int32)
+    o = ttg._opts(opts)
+    stream = torch.cuda.current_stream().cuda_stream
+    st = f(d, ranks.ctypes.data_as(C.POINTER(C.c_int32)),
+           modes.ctypes.data_as(C.POINTER(C.c_int32)), C.c_void_p(src.data_ptr()),
+           C.c_void_p(dst.data_ptr()), out_ranks.ctypes.data_as(C.POINTER(C.c_int32)),
+           C.byref(o), C.c_void_p(stream))
+    if st != 0:
+        raise ttg.TTGError(st, ttg.lib().ttg_last_error().decode())
+    out = dst.cpu().numpy()
+    res, off = [], 0
+    for k in range(d):
+        shp = (out_ranks[k], modes[k], out_ranks[k + 1])
+        n = int(np.prod(shp))
+        res.append(out[off:off + n].reshape(shp).copy())
+        off += n
+    return res
+
+
+def _inputs():
+    a = O.random([4] * 10, 8, 42, fan_in_scale=True)
+    b = O.random([4] * 10, 8, 43, fan_in_scale=True)
+    c = O.random([3, 5, 4, 6, 2], 6, 7)
+    return O.add(a, b), O.add(c, c)
+
+
+def test_noalloc_matches_allocating_round_twice(ttg):
+    t1, t2 = _inputs()
+    for t, opts in ((t1, ttg.RoundOptions(eps=1e-8)),
+                    (t2, ttg.RoundOptions(eps=1e-10, gauge=ttg.round_gauge.right_canonical))):
+        y = _noalloc_round(ttg, t, opts)
+        ref = ttg.round(t, opts)
+        assert O.ranks(y) == O.ranks(ref), (O.ranks(y), O.ranks(ref))
+        assert O.rel_err(y, ref) <= TOL
+    # the same input again after a different one: identical to the first call
+    y1 = _noalloc_round(ttg, t1, ttg.RoundOptions(eps=1e-8))
+    ref1 = ttg.round(t1, ttg.RoundOptions(eps=1e-8))
+    assert O.ranks(y1) == O.ranks(ref1) and O.rel_err(y1, ref1) <= TOL
+
+
+def test_noalloc_rejects_oversize(ttg):
+    # A TT whose work copy alone exceeds the fixed scratch is refused before
+    # any device work, with TTG_ERR_NO_SPACE and a message.
+    f = _bind(ttg)
+    d = 4
+    ranks = np.array([1, 512, 512, 512, 1], np.int32)
+    modes = np.array([8, 8, 8, 8], np.int32)
+    out_ranks = np.zeros(d + 1, np.int32)
+    o = ttg._opts(ttg.RoundOptions(eps=1e-8))
+    st = f(d, ranks.ctypes.data_as(C.POINTER(C.c_int32)),
+           modes.ctypes.data_as(C.POINTER(C.c_int32)), C.c_void_p(16), C.c_void_p(16),
+           out_ranks.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(o), None)
+    assert st == 11
+    assert b"scratch" in ttg.lib().ttg_last_error()
