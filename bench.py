@@ -43,6 +43,13 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=2)
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="batch",
+                    choices=["batch", "round_d10", "matvec_d20", "round_d40", "eval_d32"],
+                    help="batch = the headline (4096 uneven TTs); the others are the single-"
+                         "tensor configurations, measured one JSON line each")
+    ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
+    ap.add_argument("--method", choices=["svd", "svd_streaming"], default="svd")
     return ap.parse_args()
 
 
@@ -139,55 +146,67 @@ def run_ours(args):
     count = args.count
     base = SEED0 + rank * count  # weak scaling: each rank owns its own batch
     tts = make_batch(T, count, base)
-    opts = T.RoundOptions(eps=EPS)
-    plan = T.Plan("round", tts, opts=opts)
-    plan.upload(sptr)
-    torch.cuda.synchronize()
 
     def barrier():
         if world > 1:
             torch.distributed.barrier()
 
-    for _ in range(args.warmup):
-        plan.run(sptr)
-    torch.cuda.synchronize()
-    outs = plan.download(sptr)
-    bad = [r.status for r in plan.results if r.status not in (0,)]
-
-    launches0 = T.kernel_launches()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    barrier()
-    torch.cuda.synchronize()
-    with Clocks(local) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            plan.run(sptr)
-        ev1.record(stream)
+    def measure(precision):
+        """Warm-up, then exactly K timed steps of one plan; returns a dict."""
+        opts = T.RoundOptions(eps=EPS, precision=precision)
+        plan = T.Plan("round", tts, opts=opts)
+        plan.upload(sptr)
         torch.cuda.synchronize()
-    barrier()
-    launches = T.kernel_launches() - launches0
-    ms_total = ev0.elapsed_time(ev1)
-    if world > 1:
-        t = torch.tensor([ms_total], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms_total = float(t.item())
-    ms_step = ms_total / args.steps
-    value = count * world / (ms_step / 1e3)
+        for _ in range(args.warmup):
+            plan.run(sptr)
+        torch.cuda.synchronize()
+        outs = plan.download(sptr)
+        bad = [r.status for r in plan.results if r.status != 0]
+        launches0 = T.kernel_launches()
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        barrier()
+        torch.cuda.synchronize()
+        with Clocks(local) as clk:
+            ev0.record(stream)
+            for _ in range(args.steps):
+                plan.run(sptr)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        barrier()
+        launches = T.kernel_launches() - launches0
+        ms_total = ev0.elapsed_time(ev1)
+        if world > 1:
+            t = torch.tensor([ms_total], device="cuda")
+            torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+            ms_total = float(t.item())
+        kms = []
+        for _ in range(3):
+            plan.run(sptr)
+            kms.append(plan.kernel_ms())
+        io = plan.io_bytes()
+        plan.close()
+        ms_step = ms_total / args.steps
+        return {"opts": opts, "outs": outs, "bad": len(bad), "launches": launches,
+                "ms_step": ms_step, "value": count * world / (ms_step / 1e3),
+                "kernel_ms": statistics.mean(kms), "clocks": clk.summary(), "io": io}
 
-    # Kernel-only time of the sweep launch (roofline).
-    kms = []
-    for _ in range(3):
-        plan.run(sptr)
-        kms.append(plan.kernel_ms())
-    kernel_ms = statistics.mean(kms)
+    plain = measure(T.precision.fp64)
+    mixed = measure(T.precision.mixed)
+    opts = mixed["opts"]
+    outs = mixed["outs"]
+    value, ms_step, launches = mixed["value"], mixed["ms_step"], mixed["launches"]
+
     flops = 0.0
-    for t_in, t_out in zip(tts, outs):
+    for t_in, t_out in zip(tts, plain["outs"]):
         modes = [c.shape[1] for c in t_in]
         rin = [t_in[0].shape[0]] + [c.shape[-1] for c in t_in]
         rout = [t_out[0].shape[0]] + [c.shape[-1] for c in t_out]
         flops += round_flops(modes, rin, rout)
-    peak = T.device_fp64_peak()
+    peak = max(T.device_fp64_peak() for _ in range(3))
+    kernel_ms = mixed["kernel_ms"]
     achieved = flops / (kernel_ms / 1e3) / 1e12
+    plain_achieved = flops / (plain["kernel_ms"] / 1e3) / 1e12
 
     # End to end through the C-ABI with host buffers: pack + H2D + sweep +
     # D2H + unpack inside ttg_round_batch.  Inputs marshalled beforehand.
@@ -195,9 +214,9 @@ def run_ours(args):
     srcs = [T._In(t) for t in tts]
     ins = (T._Tensor * count)(*[s.t for s in srcs])
     copts = T._opts(opts)
-    h2d, d2h = plan.io_bytes()
+    h2d, d2h = mixed["io"]
     e2e_ms = []
-    for i in range(args.e2e_steps + 1):
+    for i in range(0 if args.no_e2e else args.e2e_steps + 1):
         outs_c = (T._Tensor * count)()
         torch.cuda.synchronize()
         t0 = time.perf_counter()
@@ -208,7 +227,7 @@ def run_ours(args):
         assert st == 0, T.lib().ttg_last_error()
         if i > 0:  # first call is the warm-up (pool growth)
             e2e_ms.append((t1 - t0) * 1e3)
-    e2e_step = statistics.mean(e2e_ms)
+    e2e_step = statistics.mean(e2e_ms) if e2e_ms else float("nan")
     e2e_value = count * world / (e2e_step / 1e3)
     if world > 1:
         t = torch.tensor([e2e_step], device="cuda")
@@ -218,30 +237,38 @@ def run_ours(args):
     line = {
         "metric": METRIC, "value": value, "unit": "roundings/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms_step,
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64 (QR, GEMM, refinement) + f32 (Jacobi sweeps)",
         "data": "synthetic: seeded uneven random TTs (mt19937_64 + normal_distribution)",
-        "config": dict(workload_config(count), parallelism=f"{world} independent shard(s)"),
+        "config": dict(workload_config(count), precision="mixed",
+                       parallelism=f"{world} independent shard(s)"),
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": None,
-                     "kernel": "round_kernel", "kernel_ms": kernel_ms,
+                     "kernel": "round_kernel (precision=mixed)", "kernel_ms": kernel_ms,
                      "flops_per_launch": flops,
+                     "flop_model": "algorithmic F_round (tensor_train_gb300/flops.py)",
                      "peak_source": "measured FP64 FMA loop on this GPU (ttg_device_fp64_peak)"},
+        "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_step"],
+                       "kernel_ms": plain["kernel_ms"], "achieved_tflops": plain_achieved,
+                       "frac": plain_achieved / peak, "clocks": plain["clocks"],
+                       "device_status_errors": plain["bad"]},
+        "speedup_mixed_vs_plain_fp64": plain["ms_step"] / ms_step,
         "e2e": {"value": e2e_value, "unit": "roundings/s", "h2d_bytes_per_step": h2d,
                 "d2h_bytes_per_step": d2h, "ms_per_step": e2e_step},
         "gpu_launches": launches,
-        "clocks": clk.summary(),
-        "device_status_errors": len(bad),
+        "clocks": mixed["clocks"],
+        "device_status_errors": mixed["bad"],
     }
 
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(tts, outs, args.cpu_sample)
+        line["cpu_baseline"] = cpu_baseline(tts, outs, args.cpu_sample, plain["outs"])
     if rank == 0:
         print(json.dumps(line), flush=True)
     if world > 1:
         torch.distributed.destroy_process_group()
 
 
-def cpu_baseline(tts, gpu_outs, sample):
+def cpu_baseline(tts, gpu_outs, sample, plain_outs=None):
     """The oracle (FP64 port of the reference's round) on the host cores, on
     a strided sample of the same batch; also checks the GPU outputs of the
     sampled TTs against it (ranks and relative Frobenius error)."""
@@ -250,16 +277,20 @@ def cpu_baseline(tts, gpu_outs, sample):
     idx = list(range(0, len(tts), stride))[:sample]
     threads = os.cpu_count() or 1
     sec, ref = O.round_many_timed([tts[i] for i in idx], EPS, 0, threads)
-    errs, ranks_ok = [], True
+    errs, ranks_ok, perrs = [], True, []
     for j, i in enumerate(idx[:16]):
         y = gpu_outs[i]
         yr = ref[j].cores()
         ranks_ok &= O.ranks(y) == O.ranks(yr)
         errs.append(O.rel_err(y, yr))
+        if plain_outs is not None:
+            ranks_ok &= O.ranks(plain_outs[i]) == O.ranks(yr)
+            perrs.append(O.rel_err(plain_outs[i], yr))
     return {"value": len(idx) / sec, "unit": "roundings/s", "cores": threads, "kind": "port",
             "sample": f"{len(idx)} of the {len(tts)} TTs (every {stride}th), oracle FP64 "
                       f"round on {threads} host threads, {sec:.2f} s",
             "parity_checked": len(errs), "max_rel_err_vs_oracle": max(errs),
+            "max_rel_err_plain_fp64_vs_oracle": max(perrs) if perrs else None,
             "ranks_equal": bool(ranks_ok)}
 
 
@@ -299,10 +330,146 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def single_inputs(T, workload):
+    """Seeded inputs of the single-tensor configurations (cores scaled by
+    1/sqrt(r_k n_k), or 1/sqrt(r m n) for MPO cores)."""
+    if workload == "round_d10":
+        a = T.random([4] * 10, 8, 42, fan_in_scale=True)
+        b = T.random([4] * 10, 8, 43, fan_in_scale=True)
+        return {"tt": T.add(a, b), "eps": 1e-8,
+                "desc": "round(add(a,b)): d=10, n=4, a,b random rank 8 (seeds 42/43), eps=1e-8"}
+    if workload == "round_d40":
+        a = T.random([8] * 40, 128, 46, fan_in_scale=True)
+        b = T.random([8] * 40, 128, 47, fan_in_scale=True)
+        return {"tt": T.add(T.add(a, b), T.ones([8] * 40)), "eps": 1e-8,
+                "desc": "round(a+b+ones): d=40, n=8, a,b random rank 128 (seeds 46/47), "
+                        "interior rank 257, eps=1e-8"}
+    if workload == "matvec_d20":
+        A = T.random_matrix([4] * 20, [4] * 20, 8, 44, fan_in_scale=True)
+        x = T.random([4] * 20, 32, 45, fan_in_scale=True)
+        return {"A": A, "x": x, "eps": 1e-10,
+                "desc": "matvec_round(A, x): d=20, m=n=4, MPO rank 8 (seed 44), TT rank 32 "
+                        "(seed 45), eps=1e-10"}
+    if workload == "eval_d32":
+        import numpy as np
+        t = T.random([4] * 32, 64, 48, fan_in_scale=True)
+        idx = np.random.default_rng(49).integers(0, 4, size=(1 << 20, 32)).astype(np.int32)
+        return {"tt": t, "idx": idx,
+                "desc": "eval_batch: d=32, n=4, rank 64 (seed 48), M=2^20 uniform indices "
+                        "(numpy seed 49)"}
+    raise ValueError(workload)
+
+
+def run_single(args):
+    """One JSON line for a single-tensor configuration (not the headline)."""
+    import numpy as np
+    import torch
+
+    import tensor_train_gb300 as T
+    from tensor_train_gb300.flops import eval_flops, matvec_flops, round_flops
+
+    torch.cuda.set_device(0)
+    stream = torch.cuda.current_stream()
+    sptr = stream.cuda_stream
+    inp = single_inputs(T, args.workload)
+    prec = T.precision[args.precision]
+    line = {"workload": args.workload, "config": {"workload": inp["desc"]},
+            "steps": args.steps, "warmup": args.warmup, "precision": args.precision}
+    if args.workload == "eval_d32":
+        idx_pinned = torch.from_numpy(inp["idx"]).pin_memory()
+        plan = T.Plan("eval", inp["tt"], idx_pinned)
+        unit = "evaluations/s"
+    elif args.workload == "matvec_d20":
+        opts = T.RoundOptions(eps=inp["eps"], precision=prec,
+                              method=T.round_method[args.method])
+        plan = T.Plan("matvec_round", inp["A"], inp["x"], opts=opts)
+        unit = "matvec_rounds/s"
+        line["method"] = args.method
+    else:
+        opts = T.RoundOptions(eps=inp["eps"], precision=prec)
+        plan = T.Plan("round", [inp["tt"]], opts=opts)
+        unit = "roundings/s"
+    plan.upload(sptr)
+    for _ in range(args.warmup):
+        plan.run(sptr)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with Clocks(0) as clk:
+        ev0.record(stream)
+        for _ in range(args.steps):
+            plan.run(sptr)
+        ev1.record(stream)
+        torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1) / args.steps
+    if args.workload == "eval_d32":
+        M = inp["idx"].shape[0]
+        out = plan.download(sptr)
+        ranks = [inp["tt"][0].shape[0]] + [c.shape[-1] for c in inp["tt"]]
+        F = eval_flops(ranks, M)
+        nbytes = 4 * inp["idx"].size + 8 * M + 8 * sum(c.size for c in inp["tt"])
+        line.update({"value": M / (ms / 1e3), "unit": unit, "ms_per_step": ms,
+                     "roofline": {"bound": "fp64", "achieved": F / (ms / 1e3) / 1e12,
+                                  "peak": max(T.device_fp64_peak() for _ in range(3)),
+                                  "unit": "TFLOP/s", "hbm_gbs": nbytes / (ms / 1e3) / 1e9,
+                                  "bytes_per_launch": nbytes, "flops_per_launch": F}})
+        line["roofline"]["frac"] = line["roofline"]["achieved"] / line["roofline"]["peak"]
+        from oracle import pyoracle as O
+        sel = np.arange(0, M, M // 4096)
+        t0 = time.perf_counter()
+        ref = O.eval_batch(inp["tt"], inp["idx"][sel])
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": len(sel) / sec, "unit": unit, "cores": 1,
+                                "kind": "port", "sample": f"{len(sel)} of the {M} indices"}
+        line["parity_max_abs_err"] = float(np.max(np.abs(out[sel] - ref)))
+    else:
+        kms = []
+        for _ in range(3):
+            plan.run(sptr)
+            kms.append(plan.kernel_ms())
+        outs = plan.download(sptr)
+        y = outs[0]
+        rout = [y[0].shape[0]] + [c.shape[-1] for c in y]
+        if args.workload == "matvec_d20":
+            A, x = inp["A"], inp["x"]
+            ra = [A[0].shape[0]] + [c.shape[-1] for c in A]
+            rx = [x[0].shape[0]] + [c.shape[-1] for c in x]
+            rin = [a * b for a, b in zip(ra, rx)]
+            modes = [c.shape[1] for c in A]
+            F = matvec_flops(ra, rx, modes, [c.shape[2] for c in A]) + \
+                round_flops(modes, rin, rout)
+        else:
+            t = inp["tt"]
+            modes = [c.shape[1] for c in t]
+            F = round_flops(modes, [t[0].shape[0]] + [c.shape[-1] for c in t], rout)
+        peak = max(T.device_fp64_peak() for _ in range(3))
+        kernel_ms = statistics.mean(kms)
+        line.update({"value": 1e3 / ms, "unit": unit, "ms_per_step": ms, "ranks_out": rout,
+                     "roofline": {"bound": "fp64", "achieved": F / (kernel_ms / 1e3) / 1e12,
+                                  "peak": peak, "unit": "TFLOP/s", "kernel_ms": kernel_ms,
+                                  "flops_per_launch": F}})
+        line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
+        if not args.no_cpu_baseline:
+            from oracle import pyoracle as O
+            t0 = time.perf_counter()
+            if args.workload == "matvec_d20":
+                ref = O.matvec_round(inp["A"], inp["x"], inp["eps"], method=args.method)
+            else:
+                ref = O.round(inp["tt"], inp["eps"])
+            sec = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": 1.0 / sec, "unit": unit, "cores": 1,
+                                    "kind": "port", "sample": "one full call (oracle, 1 thread)"}
+            line["parity"] = {"ranks_equal": O.ranks(ref) == rout,
+                              "rel_err_vs_oracle": O.rel_err(y, ref)}
+    line["clocks"] = clk.summary()
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload != "batch":
+        run_single(args)
     else:
         run_ours(args)
 

@@ -57,7 +57,11 @@ typedef enum ttg_method {
 /* round_gauge (round/round.hpp:49-53). */
 typedef enum ttg_gauge { TTG_GAUGE_NONE = 0, TTG_GAUGE_RIGHT_CANONICAL = 1 } ttg_gauge;
 
-/* Arithmetic of the bulk contractions.  FP64 is the plain rounder. */
+/* Arithmetic of the sweeps.  FP64: every operation in FP64 (the plain
+ * rounder).  MIXED: the Jacobi SVD sweeps run in FP32 and one FP64
+ * refinement (Newton-Schulz re-orthogonalisation of the FP32 rotations, then
+ * FP64 Jacobi polish) restores FP64 accuracy of the singular vectors and
+ * values; QR and contractions stay FP64. */
 typedef enum ttg_precision { TTG_PREC_FP64 = 0, TTG_PREC_MIXED = 1 } ttg_precision;
 
 /* round_options (round/round.hpp:55-105), SVD-relevant fields plus the

@@ -224,6 +224,7 @@ struct ttg_plan
   int64_t arena_doubles = 0;
   int64_t scratch_stride = 0;
   int grid = 1;
+  int smem_doubles = 0;
   // products computed on the device before the sweep (naive apply-round):
   struct Apply
   {
@@ -338,8 +339,19 @@ double est_cost(const Shape& s)
   return c;
 }
 
+// Dynamic shared memory of the sweep kernel: two CTAs per SM share the
+// SM's 228 KB (each also has ~17 KB of static shared state) when the grid
+// is larger than the SM count, one CTA gets ~200 KB otherwise.
+constexpr int kSmemTwoPerSm = 11776;  // 92 KB
+constexpr int kSmemOnePerSm = 25600;  // 200 KB
+
 int32_t layout_and_alloc(ttg_plan& P)
 {
+  static const cudaError_t optin = round_smem_optin(kSmemOnePerSm);
+  if (optin != cudaSuccess)
+    return fail(TTG_ERR_CUDA, std::string("round kernel shared-memory opt-in: ") +
+                                  cudaGetErrorString(optin));
+  P.smem_doubles = P.grid > std::max(device().sms, 1) ? kSmemTwoPerSm : kSmemOnePerSm;
   size_t o = 0;
   P.off_arena = o;
   o = align256(o + sizeof(double) * static_cast<size_t>(P.arena_doubles));
@@ -411,6 +423,8 @@ RoundJob make_job(ttg_plan& P)
   j.eps = P.opts.eps;
   j.max_rank = P.opts.max_rank;
   j.max_sweeps = P.opts.max_sweeps > 0 ? P.opts.max_sweeps : 40;
+  j.smem_doubles = P.smem_doubles;
+  j.mixed = P.opts.precision == TTG_PREC_MIXED ? 1 : 0;
   j.a_idx = reinterpret_cast<const int32_t*>(d + P.off_aidx);
   j.b_idx = reinterpret_cast<const int32_t*>(d + P.off_bidx);
   j.out_idx = reinterpret_cast<const int32_t*>(d + P.off_oidx);
@@ -427,8 +441,8 @@ int32_t check_opts(const ttg_round_options* o, const char* op)
     return fail(TTG_ERR_ARG, std::string(op) + ": max_rank must be >= 0");
   if (o->gauge != TTG_GAUGE_NONE && o->gauge != TTG_GAUGE_RIGHT_CANONICAL)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown gauge");
-  if (o->precision != TTG_PREC_FP64)
-    return fail(TTG_ERR_METHOD, std::string(op) + ": only precision FP64 is served by this build");
+  if (o->precision != TTG_PREC_FP64 && o->precision != TTG_PREC_MIXED)
+    return fail(TTG_ERR_ARG, std::string(op) + ": unknown precision");
   if (o->method == TTG_METHOD_ALS || o->method == TTG_METHOD_DMRG)
     return fail(TTG_ERR_METHOD, std::string(op) + ": als/dmrg rounding is not served here");
   if (o->method < 0 || o->method > TTG_METHOD_DMRG)

@@ -40,13 +40,27 @@ struct CtaShared
   double dval[4];
 };
 
-__device__ __forceinline__ double warp_sum(double v)
+template <class T>
+__device__ __forceinline__ T warp_sum(T v)
 {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1)
     v += __shfl_xor_sync(0xffffffffu, v, o);
   return v;
 }
+
+template <class T>
+struct Eps;
+template <>
+struct Eps<double>
+{
+  static __device__ __forceinline__ double value() { return DBL_EPSILON; }
+};
+template <>
+struct Eps<float>
+{
+  static __device__ __forceinline__ float value() { return 4.0f * FLT_EPSILON; }
+};
 
 // Sum over the CTA; every thread gets the same value (the partials are
 // added in a fixed order by every thread).
@@ -233,16 +247,20 @@ __device__ void cta_apply_q(const double* A, int m, int kref, int64_t lda, const
 // V column-major (n x n, ldv) accumulates the rotations when non-null (it
 // must hold the identity, or any start matrix, on entry).  Pairs are visited
 // in the round-robin tournament order, n/2 disjoint pairs per round, one
-// warp per pair.  Returns the number of sweeps; *converged = 0 if the limit
-// was reached.  Rotation as in Demmel & Veselic (1992), eq. (4.3).
+// warp per pair.  Squared column norms are cached in nrm[n] (recomputed at
+// the start of every sweep, updated after each rotation as
+// alpha' = alpha - t*gamma, beta' = beta + t*gamma), so a pair costs one dot
+// product and one rotation.  Returns the number of sweeps; *converged = 0 if
+// the limit was reached.  Rotation as in Demmel & Veselic (1992), eq. (4.3).
 // ---------------------------------------------------------------------------
-__device__ int cta_jacobi(double* A, int m, int n, int64_t lda, double* V, int64_t ldv,
-                          int max_sweeps, int* converged, CtaShared& sh)
+template <class T>
+__device__ int cta_jacobi(T* A, int m, int n, int64_t lda, T* V, int64_t ldv, int max_sweeps,
+                          int* converged, T* nrm, CtaShared& sh)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int N = n + (n & 1);
   const int npairs = N / 2;
-  const double tol = sqrt(static_cast<double>(m > 1 ? m : 1)) * DBL_EPSILON;
+  const T tol = sqrt(static_cast<T>(m > 1 ? m : 1)) * Eps<T>::value();
   int sweep = 0;
   *converged = 0;
   if (n < 2)
@@ -255,6 +273,16 @@ __device__ int cta_jacobi(double* A, int m, int n, int64_t lda, double* V, int64
     __syncthreads();
     if (threadIdx.x == 0)
       sh.flag = 0;
+    for (int j = w; j < n; j += kWarps)
+    {
+      const T* a = A + j * lda;
+      T s = 0;
+      for (int i = lane; i < m; i += 32)
+        s += a[i] * a[i];
+      s = warp_sum(s);
+      if (lane == 0)
+        nrm[j] = s;
+    }
     __syncthreads();
     for (int r = 0; r < N - 1; ++r)
     {
@@ -270,48 +298,46 @@ __device__ int cta_jacobi(double* A, int m, int n, int64_t lda, double* V, int64
           p = q;
           q = tmp;
         }
-        double* ap = A + p * lda;
-        double* aq = A + q * lda;
-        double al = 0.0, be = 0.0, ga = 0.0;
+        T* ap = A + p * lda;
+        T* aq = A + q * lda;
+        const T al = nrm[p], be = nrm[q];
+        T ga = 0;
         for (int i = lane; i < m; i += 32)
-        {
-          const double x = ap[i], y = aq[i];
-          al += x * x;
-          be += y * y;
-          ga += x * y;
-        }
-        al = warp_sum(al);
-        be = warp_sum(be);
+          ga += ap[i] * aq[i];
         ga = warp_sum(ga);
-        if (ga == 0.0 || fabs(ga) <= tol * sqrt(al * be))
+        if (ga == T(0) || fabs(ga) <= tol * sqrt(fmax(al, T(0)) * fmax(be, T(0))))
           continue;
-        const double zeta = (be - al) / (2.0 * ga);
-        double tt;
-        if (fabs(zeta) > 1.0e150)
-          tt = 0.5 / zeta;
+        const T zeta = (be - al) / (T(2) * ga);
+        T tt;
+        if (fabs(zeta) > T(1.0e18))
+          tt = T(0.5) / zeta;
         else
-          tt = (zeta >= 0.0 ? 1.0 : -1.0) / (fabs(zeta) + sqrt(1.0 + zeta * zeta));
-        const double c = 1.0 / sqrt(1.0 + tt * tt);
-        const double s = c * tt;
+          tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
+        const T c = T(1) / sqrt(T(1) + tt * tt);
+        const T s = c * tt;
         for (int i = lane; i < m; i += 32)
         {
-          const double x = ap[i], y = aq[i];
+          const T x = ap[i], y = aq[i];
           ap[i] = c * x - s * y;
           aq[i] = s * x + c * y;
         }
         if (V)
         {
-          double* vp = V + p * ldv;
-          double* vq = V + q * ldv;
+          T* vp = V + p * ldv;
+          T* vq = V + q * ldv;
           for (int i = lane; i < n; i += 32)
           {
-            const double x = vp[i], y = vq[i];
+            const T x = vp[i], y = vq[i];
             vp[i] = c * x - s * y;
             vq[i] = s * x + c * y;
           }
         }
         if (lane == 0)
+        {
+          nrm[p] = al - tt * ga;
+          nrm[q] = be + tt * ga;
           sh.flag = 1;
+        }
       }
       __syncthreads();
     }
@@ -443,6 +469,55 @@ __device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t
         }
     }
   __syncthreads();
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision one-sided Jacobi: the sweeps that do most of the rotating
+// run in FP32, one FP64 refinement restores FP64 accuracy.
+//   1. FP32 copy of src (m x n, m >= n) and V32 = I in fbuf
+//      (m*n + n*n floats); FP32 Jacobi sweeps accumulate V32.
+//   2. V = V32 * (3I - V32^T V32)/2 in FP64 (one Newton-Schulz step: V is
+//      orthogonal to FP64 accuracy), in tmp (3 n*n doubles).
+//   3. A = src * V (FP64 GEMM) -- nearly orthogonal columns.
+//   4. FP64 Jacobi sweeps on A (typically one rotating sweep and one check);
+//      when Vout is given it starts from V and accumulates the rotations.
+// src stays readable throughout; fbuf may alias A (it is dead before step 3).
+// Returns the FP64 sweep count.
+// ---------------------------------------------------------------------------
+__device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
+                                int max_sweeps, int* converged, double* nrm, float* fbuf,
+                                double* tmp, CtaShared& sh)
+{
+  float* Af = fbuf;
+  float* Vf = fbuf + static_cast<int64_t>(m) * n;
+  const int64_t mn = static_cast<int64_t>(m) * n, nn = static_cast<int64_t>(n) * n;
+  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
+    Af[t] = static_cast<float>(src(t % m, t / m));
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    Vf[t] = (t % n == t / n) ? 1.0f : 0.0f;
+  __syncthreads();
+  int conv32 = 0;
+  cta_jacobi<float>(Af, m, n, m, Vf, n, 24, &conv32, reinterpret_cast<float*>(nrm), sh);
+  double* Vd = tmp;
+  double* P = tmp + nn;
+  double* V2 = tmp + 2 * nn;
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    Vd[t] = static_cast<double>(Vf[t]);
+  __syncthreads();
+  // P = Vd^T Vd ; P <- (3I - P)/2 ; V2 = Vd P.
+  cta_gemm(n, n, n, View{Vd, n, 1}, View{Vd, 1, n}, P, 1, n, sh);
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    P[t] = ((t % n == t / n) ? 1.5 : 0.0) - 0.5 * P[t];
+  __syncthreads();
+  cta_gemm(n, n, n, View{Vd, 1, n}, View{P, 1, n}, V2, 1, n, sh);
+  cta_gemm(m, n, n, src, View{V2, 1, n}, A, 1, lda, sh);
+  if (Vout)
+  {
+    for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+      Vout[t] = V2[t];
+    __syncthreads();
+  }
+  return cta_jacobi<double>(A, m, n, lda, Vout, n, max_sweeps, converged, nrm, sh);
 }
 
 }  // namespace ttg

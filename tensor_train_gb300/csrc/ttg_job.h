@@ -28,7 +28,11 @@ TTG_HD inline int64_t imax64(int64_t a, int64_t b) { return a > b ? a : b; }
 // left_svd on an (h x c) matrix, all three branches.
 TTG_HD inline int64_t need_left_svd(int64_t h, int64_t c)
 {
-  return 2 * a32(h * c) + 4 * a32(c * c) + 2 * a32(h * h) + 4 * a32(imax64(h, c));
+  const int64_t mn = h < c ? h : c;
+  // + FP32 staging (m*n + n*n floats) and 3 n*n FP64 temporaries of the
+  // mixed-precision Jacobi (n = min(h, c)).
+  return 2 * a32(h * c) + 4 * a32(c * c) + 2 * a32(h * h) + 6 * a32(imax64(h, c)) +
+         a32(h * c) + 4 * a32(mn * mn);
 }
 // right_qr_step on a core (r, w = n*rp) with previous core of h_prev rows.
 TTG_HD inline int64_t need_right_qr(int64_t r, int64_t w, int64_t h_prev)
@@ -102,6 +106,8 @@ struct RoundJob
   double eps;
   int32_t max_rank;
   int32_t max_sweeps;
+  int32_t smem_doubles;  // dynamic shared memory per CTA (doubles) for staging
+  int32_t mixed;         // 1: FP32 Jacobi sweeps + FP64 refinement in the SVD steps
   // Streaming jobs: item i rounds the product of TT a_idx[i] (operator) and
   // b_idx[i] (operand) into output TT out_idx[i].  Row/col modes of the
   // operator cores come from CoreSlot::m and n/m.

@@ -53,10 +53,22 @@ __device__ void set_status(TTInfo& T, int st)
     T.status = st;
 }
 
-// QR of X (h x c).  Q -> W (h x k, column-major, ld h), R -> R (k x c,
-// column-major, ld k), k = min(h, c).
-__device__ int qr_factor(View X, int h, int c, double* W, double* tau, double* R, CtaShared& sh)
+// Dynamic shared memory of the CTA, used to stage the matrix a step works
+// on when it fits (cap doubles).
+struct Smem
 {
+  double* p;
+  int64_t cap;
+};
+
+// QR of X (h x c).  Q -> *W (h x k, column-major, ld h), R -> R (k x c,
+// column-major, ld k), k = min(h, c).  The factorisation runs in shared
+// memory when h*c fits there, else in Wg; *W tells the caller where Q is.
+__device__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* R, Smem sm,
+                         double** Wout, CtaShared& sh)
+{
+  double* W = (static_cast<int64_t>(h) * c <= sm.cap) ? sm.p : Wg;
+  *Wout = W;
   cta_copy_to_colmajor(W, h, X, h, c);
   __syncthreads();
   cta_householder_qr(W, h, c, h, tau, sh);
@@ -74,7 +86,8 @@ __device__ int qr_factor(View X, int h, int c, double* W, double* tau, double* R
 // otherwise decompose X directly -- by columns when h >= c, by rows (the
 // transpose, accumulating V) when h < c.
 __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
-                        Bump bump, double** Ut_out, double** F_out, TTInfo& T, CtaShared& sh)
+                        bool mixed, Bump bump, Smem sm, double** Ut_out, double** F_out,
+                        TTInfo& T, CtaShared& sh)
 {
   double* sig;
   double* sorted;
@@ -91,17 +104,39 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     sig = bump.take(c);
     sorted = bump.take(c);
     ord = reinterpret_cast<int*>(bump.take(c));
+    double* nrm = bump.take(c);
     double* Uc = bump.take(static_cast<int64_t>(c) * c);
     U = bump.take(static_cast<int64_t>(h) * c);
     F = bump.take(static_cast<int64_t>(c) * c);
+    // Shared-memory staging: the Jacobi matrix first (it is touched most),
+    // then the Householder panel when both fit.
+    const int64_t cc = static_cast<int64_t>(c) * c, hc = static_cast<int64_t>(h) * c;
+    if (cc + c <= sm.cap)
+    {
+      A = sm.p;
+      nrm = sm.p + cc;
+      if (hc + cc + c <= sm.cap)
+        W = sm.p + cc + c;
+    }
+    const bool A_in_smem = (A == sm.p);
     cta_copy_to_colmajor(W, h, X, h, c);
     __syncthreads();
     cta_householder_qr(W, h, c, h, tau, sh);
     cta_extract_r(R, W, c, c, h);
-    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(c) * c; t += blockDim.x)
-      A[t] = R[t];
-    __syncthreads();
-    sweeps = cta_jacobi(A, c, c, c, nullptr, 0, max_sweeps, &conv, sh);
+    if (mixed)
+    {
+      float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(cc));
+      double* tmp = bump.take(3 * cc);
+      sweeps = cta_jacobi_mixed(View{R, 1, c}, c, c, A, c, nullptr, max_sweeps, &conv, nrm, fbuf,
+                                tmp, sh);
+    }
+    else
+    {
+      for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+        A[t] = R[t];
+      __syncthreads();
+      sweeps = cta_jacobi<double>(A, c, c, c, nullptr, 0, max_sweeps, &conv, nrm, sh);
+    }
     cta_col_norms(A, c, c, c, sig);
     cta_argsort_desc(sig, c, ord, sorted);
     if (threadIdx.x == 0)
@@ -145,11 +180,29 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     sig = bump.take(c);
     sorted = bump.take(c);
     ord = reinterpret_cast<int*>(bump.take(c));
+    double* nrm = bump.take(c);
     U = bump.take(static_cast<int64_t>(h) * c);
     F = bump.take(static_cast<int64_t>(c) * c);
-    cta_copy_to_colmajor(A, h, X, h, c);
-    __syncthreads();
-    sweeps = cta_jacobi(A, h, c, h, nullptr, 0, max_sweeps, &conv, sh);
+    const int64_t hc = static_cast<int64_t>(h) * c;
+    bool A_in_smem = false;
+    if (hc + c <= sm.cap)
+    {
+      A = sm.p;
+      nrm = sm.p + hc;
+      A_in_smem = true;
+    }
+    if (mixed)
+    {
+      float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(hc));
+      double* tmp = bump.take(3 * static_cast<int64_t>(c) * c);
+      sweeps = cta_jacobi_mixed(X, h, c, A, h, nullptr, max_sweeps, &conv, nrm, fbuf, tmp, sh);
+    }
+    else
+    {
+      cta_copy_to_colmajor(A, h, X, h, c);
+      __syncthreads();
+      sweeps = cta_jacobi<double>(A, h, c, h, nullptr, 0, max_sweeps, &conv, nrm, sh);
+    }
     cta_col_norms(A, h, c, h, sig);
     cta_argsort_desc(sig, c, ord, sorted);
     if (threadIdx.x == 0)
@@ -186,13 +239,33 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
   sig = bump.take(h);
   sorted = bump.take(h);
   ord = reinterpret_cast<int*>(bump.take(h));
+  double* nrm = bump.take(h);
   U = bump.take(static_cast<int64_t>(h) * h);
   F = bump.take(static_cast<int64_t>(h) * c);
-  cta_copy_to_colmajor(A, c, transposed(X), c, h);
-  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * h; t += blockDim.x)
-    V[t] = (t % h == t / h) ? 1.0 : 0.0;
-  __syncthreads();
-  sweeps = cta_jacobi(A, c, h, c, V, h, max_sweeps, &conv, sh);
+  const int64_t ch = static_cast<int64_t>(c) * h, hh = static_cast<int64_t>(h) * h;
+  bool A_in_smem = false;
+  if (ch + h <= sm.cap)
+  {
+    A = sm.p;
+    nrm = sm.p + ch;
+    A_in_smem = true;
+    if (ch + h + hh <= sm.cap)
+      V = sm.p + ch + h;
+  }
+  if (mixed)
+  {
+    float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(ch));
+    double* tmp = bump.take(3 * hh);
+    sweeps = cta_jacobi_mixed(transposed(X), c, h, A, c, V, max_sweeps, &conv, nrm, fbuf, tmp, sh);
+  }
+  else
+  {
+    cta_copy_to_colmajor(A, c, transposed(X), c, h);
+    for (int64_t t = threadIdx.x; t < hh; t += blockDim.x)
+      V[t] = (t % h == t / h) ? 1.0 : 0.0;
+    __syncthreads();
+    sweeps = cta_jacobi<double>(A, c, h, c, V, h, max_sweeps, &conv, nrm, sh);
+  }
   cta_col_norms(A, c, h, c, sig);
   cta_argsort_desc(sig, h, ord, sorted);
   if (threadIdx.x == 0)
@@ -242,7 +315,8 @@ __device__ void set_ranks(CoreSlot& s, int r, int rp)
 
 // right_qr_step (detail/orthogonalize.hpp:63-100): QR of M^T (n*rp x r);
 // r_eff = min(n*rp, r); L = R^T absorbed into prev.
-__device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bump, CtaShared& sh)
+__device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bump, Smem sm,
+                              CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
   const int w = n * rp;
@@ -253,18 +327,20 @@ __device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bu
   double* tau = bump.take(r);
   double* R = bump.take(static_cast<int64_t>(r) * r);
   double* P = bump.take(static_cast<int64_t>(hp) * r);
-  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sh);
+  double* Q;
+  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sm, &Q, sh);
   // prev (hp x k) = left_unfold(prev) (hp x r) * L, L(a, e) = R(e, a).
   cta_gemm(hp, k, r, View{ps, r, 1}, View{R, k, 1}, P, k, 1, sh);
   cta_copy(ps, P, static_cast<int64_t>(hp) * k);
-  cta_copy(cs, W, static_cast<int64_t>(w) * k);
+  cta_copy(cs, Q, static_cast<int64_t>(w) * k);
   set_ranks(cur, k, rp);
   set_ranks(prev, prev.r, k);
   __syncthreads();
 }
 
 // left_qr_step (detail/orthogonalize.hpp:35-60).
-__device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bump, CtaShared& sh)
+__device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bump, Smem sm,
+                             CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
   const int h = r * n;
@@ -275,12 +351,13 @@ __device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bum
   double* tau = bump.take(rp);
   double* R = bump.take(static_cast<int64_t>(rp) * rp);
   double* P = bump.take(static_cast<int64_t>(rp) * wn);
-  const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sh);
+  double* Q;
+  const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sm, &Q, sh);
   // next (k x wn) = R (k x rp) * right_unfold(next) (rp x wn).
   cta_gemm(k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, P, wn, 1, sh);
   cta_copy(ns, P, static_cast<int64_t>(k) * wn);
   // cur row-major (h x k) <- Q column-major.
-  cta_copy_to_rowmajor(cs, k, View{W, 1, h}, h, k);
+  cta_copy_to_rowmajor(cs, k, View{Q, 1, h}, h, k);
   set_ranks(cur, r, k);
   set_ranks(next, k, next.rp);
   __syncthreads();
@@ -288,7 +365,7 @@ __device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bum
 
 // svd_step (detail/truncate.hpp:61-99).
 __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& next,
-                         double delta, Bump bump, TTInfo& T, CtaShared& sh)
+                         double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, c = cur.rp;
   const int h = r * n;
@@ -297,8 +374,8 @@ __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlo
   double* ns = ar + next.off;
   double* P = bump.take(static_cast<int64_t>(c) * wn);
   double *U, *F;
-  const int r_new = left_svd(View{cs, c, 1}, h, c, delta, job.max_rank, job.max_sweeps, bump, &U,
-                             &F, T, sh);
+  const int r_new = left_svd(View{cs, c, 1}, h, c, delta, job.max_rank, job.max_sweeps,
+                             job.mixed != 0, bump, sm, &U, &F, T, sh);
   cta_gemm(r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, P, wn, 1, sh);
   cta_copy(ns, P, static_cast<int64_t>(r_new) * wn);
   cta_copy_to_rowmajor(cs, r_new, View{U, 1, h}, h, r_new);
@@ -309,7 +386,7 @@ __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlo
 
 // svd_step_right (detail/truncate.hpp:114-166) as a left step on M^T.
 __device__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& prev,
-                               double delta, Bump bump, TTInfo& T, CtaShared& sh)
+                               double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
   const int w = n * rp;
@@ -318,8 +395,8 @@ __device__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, C
   double* ps = ar + prev.off;
   double* P = bump.take(static_cast<int64_t>(hp) * r);
   double *U, *F;
-  const int r_new = left_svd(View{cs, 1, w}, w, r, delta, job.max_rank, job.max_sweeps, bump, &U,
-                             &F, T, sh);
+  const int r_new = left_svd(View{cs, 1, w}, w, r, delta, job.max_rank, job.max_sweeps,
+                             job.mixed != 0, bump, sm, &U, &F, T, sh);
   // prev (hp x r_new) = left_unfold(prev) (hp x r) * F^T.
   cta_gemm(hp, r_new, r, View{ps, r, 1}, View{F, 1, r}, P, r_new, 1, sh);
   cta_copy(ps, P, static_cast<int64_t>(hp) * r_new);
@@ -445,7 +522,7 @@ __device__ int64_t balance_need(const CoreSlot* S, int d)
   return a32(total + 1);
 }
 
-__device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShared& sh)
+__device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh)
 {
   TTInfo& T = job.tts[tti];
   const int d = T.d;
@@ -460,7 +537,7 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShare
       if (!fits(job, need_right_qr(S[k].r, static_cast<int64_t>(S[k].n) * S[k].rp,
                                    static_cast<int64_t>(S[k - 1].r) * S[k - 1].n), T))
         return;
-      right_qr_step(ar, S[k], S[k - 1], Bump{scratch}, sh);
+      right_qr_step(ar, S[k], S[k - 1], Bump{scratch}, sm, sh);
     }
     if (job.kind == kJobRightOrth)
       return;
@@ -485,7 +562,7 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShare
       if (!fits(job, need_svd_step(static_cast<int64_t>(S[k].r) * S[k].n, S[k].rp,
                                    static_cast<int64_t>(S[k + 1].n) * S[k + 1].rp), T))
         return;
-      svd_step(job, ar, S[k], S[k + 1], delta, Bump{scratch}, T, sh);
+      svd_step(job, ar, S[k], S[k + 1], delta, Bump{scratch}, sm, T, sh);
     }
     if (!fits(job, balance_need(S, d), T))
       return;
@@ -498,7 +575,7 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShare
     if (!fits(job, need_left_qr(static_cast<int64_t>(S[k].r) * S[k].n, S[k].rp,
                                 static_cast<int64_t>(S[k + 1].n) * S[k + 1].rp), T))
       return;
-    left_qr_step(ar, S[k], S[k + 1], Bump{scratch}, sh);
+    left_qr_step(ar, S[k], S[k + 1], Bump{scratch}, sm, sh);
   }
   const double nrm = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
   if (threadIdx.x == 0)
@@ -521,13 +598,13 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, CtaShare
     if (!fits(job, need_svd_step_right(static_cast<int64_t>(S[k].n) * S[k].rp, S[k].r,
                                        static_cast<int64_t>(S[k - 1].r) * S[k - 1].n), T))
       return;
-    svd_step_right(job, ar, S[k], S[k - 1], delta, Bump{scratch}, T, sh);
+    svd_step_right(job, ar, S[k], S[k - 1], delta, Bump{scratch}, sm, T, sh);
   }
 }
 
 // build_streaming_matvec / build_streaming_matmat
 // (detail/streaming_apply.hpp:39-202) for one (operator, operand) pair.
-__device__ void stream_tt(const RoundJob& job, int item, double* scratch, CtaShared& sh)
+__device__ void stream_tt(const RoundJob& job, int item, double* scratch, Smem sm, CtaShared& sh)
 {
   double* ar = job.arena;
   TTInfo& TA = job.tts[job.a_idx[item]];
@@ -542,14 +619,14 @@ __device__ void stream_tt(const RoundJob& job, int item, double* scratch, CtaSha
     if (!fits(job, need_right_qr(SA[k].r, static_cast<int64_t>(SA[k].n) * SA[k].rp,
                                  static_cast<int64_t>(SA[k - 1].r) * SA[k - 1].n), TO))
       return;
-    right_qr_step(ar, SA[k], SA[k - 1], Bump{scratch}, sh);
+    right_qr_step(ar, SA[k], SA[k - 1], Bump{scratch}, sm, sh);
   }
   for (int k = d - 1; k >= 1; --k)
   {
     if (!fits(job, need_right_qr(SX[k].r, static_cast<int64_t>(SX[k].n) * SX[k].rp,
                                  static_cast<int64_t>(SX[k - 1].r) * SX[k - 1].n), TO))
       return;
-    right_qr_step(ar, SX[k], SX[k - 1], Bump{scratch}, sh);
+    right_qr_step(ar, SX[k], SX[k - 1], Bump{scratch}, sm, sh);
   }
   const double nA = core_norm(ar + SA[0].off, core_size(SA[0]), sh);
   const double nX = core_norm(ar + SX[0].off, core_size(SX[0]), sh);
@@ -654,7 +731,7 @@ __device__ void stream_tt(const RoundJob& job, int item, double* scratch, CtaSha
     }
     double *U, *F;
     const int r_new = left_svd(View{Cj, ccols, 1}, hrows, ccols, delta, job.max_rank,
-                               job.max_sweeps, bump, &U, &F, TO, sh);
+                               job.max_sweeps, job.mixed != 0, bump, sm, &U, &F, TO, sh);
     cta_copy_to_rowmajor(os, r_new, View{U, 1, hrows}, hrows, r_new);
     cta_copy(Fbuf, F, static_cast<int64_t>(r_new) * ccols);
     set_ranks(SO[k], alpha, r_new);
@@ -668,6 +745,8 @@ __device__ void stream_tt(const RoundJob& job, int item, double* scratch, CtaSha
 __global__ void __launch_bounds__(kThreads) round_kernel(RoundJob job)
 {
   __shared__ CtaShared sh;
+  extern __shared__ double dyn_smem[];
+  const Smem sm{dyn_smem, job.smem_doubles};
   double* scratch = job.scratch + static_cast<int64_t>(blockIdx.x) * job.scratch_stride;
   for (;;)
   {
@@ -679,9 +758,9 @@ __global__ void __launch_bounds__(kThreads) round_kernel(RoundJob job)
     if (item >= job.ntt)
       break;
     if (job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat)
-      stream_tt(job, job.order[item], scratch, sh);
+      stream_tt(job, job.order[item], scratch, sm, sh);
     else
-      round_tt(job, job.order[item], scratch, sh);
+      round_tt(job, job.order[item], scratch, sm, sh);
   }
 }
 
@@ -817,7 +896,14 @@ __global__ void __launch_bounds__(kThreads) inner_kernel(const double* __restric
 
 void launch_round(const RoundJob& job, int grid, cudaStream_t stream)
 {
-  round_kernel<<<grid, kThreads, 0, stream>>>(job);
+  const size_t smem = sizeof(double) * static_cast<size_t>(job.smem_doubles);
+  round_kernel<<<grid, kThreads, smem, stream>>>(job);
+}
+
+cudaError_t round_smem_optin(int smem_doubles)
+{
+  return cudaFuncSetAttribute(round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                              static_cast<int>(sizeof(double) * smem_doubles));
 }
 
 void launch_apply_core(const double* A, const double* X, double* Y, int r, int m, int p, int rp,

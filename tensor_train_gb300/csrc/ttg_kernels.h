@@ -18,6 +18,7 @@ void launch_eval(const double* ar, const CoreSlot* S, int d, const int* idx, int
 void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int d,
                   double* scratch, int64_t env_cap, double* out, cudaStream_t stream);
 cudaError_t eval_smem_optin(int rcap);
+cudaError_t round_smem_optin(int smem_doubles);
 void launch_fp64_peak(double* out, int iters, int grid, int block, cudaStream_t stream);
 // Sets the message returned by ttg_last_error() on this thread.
 void set_last_error(const std::string& msg);

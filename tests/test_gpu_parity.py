@@ -217,3 +217,57 @@ def test_errors(ttg):
         ttg.matvec_round(A, O.random([2, 2], 2, 2),
                          ttg.RoundOptions(method=ttg.round_method.svd_naive))
     assert e.value.status == 3
+
+
+# -- mixed precision (FP32 Jacobi sweeps + FP64 refinement) -------------------
+# Bar from the task: relative error <= 1e-8 against the FP64 oracle and ranks
+# within +/-1 per bond; the FP64 refinement is expected to land far below.
+MIXED_TOL = 1e-10
+
+
+def _mixed(ttg, **kw):
+    return ttg.RoundOptions(precision=ttg.precision.mixed, **kw)
+
+
+def test_mixed_round_config1(ttg):
+    t = cfg1()
+    y = ttg.round(t, _mixed(ttg, eps=1e-8))
+    _close(y, O.round(t, 1e-8), MIXED_TOL)
+
+
+def test_mixed_round_truncating_and_gauges(ttg):
+    a = O.random([4, 5, 6, 4], 6, 13)
+    b = _inflate(a, 5)
+    y = ttg.round(b, _mixed(ttg, eps=1e-10))
+    _close(y, O.round(b, 1e-10), MIXED_TOL)
+    t = O.add(O.random([4] * 6, 6, 1), O.random([4] * 6, 6, 2))
+    y = ttg.round(t, _mixed(ttg, eps=1e-10, gauge=ttg.round_gauge.right_canonical))
+    _close(y, O.round(t, 1e-10, gauge="right_canonical"), MIXED_TOL)
+    a = O.random([2, 3, 4, 2], 8, 99)
+    y = ttg.round(a, _mixed(ttg, eps=0.01))
+    _close(y, O.round(a, 0.01), MIXED_TOL)
+
+
+def test_mixed_batch_uneven(ttg):
+    tts = [O.random_uneven(2000 + i, 8, 20, 4, 64) for i in range(16)]
+    ys = ttg.round_batch(tts, _mixed(ttg, eps=1e-8))
+    for t, y in zip(tts, ys):
+        _close(y, O.round(t, 1e-8), MIXED_TOL)
+
+
+def test_mixed_matvec_round(ttg):
+    A = O.random_matrix([4] * 5, [4] * 5, 8, 44, fan_in_scale=True)
+    x = O.random([4] * 5, 16, 45, fan_in_scale=True)
+    for method in ("svd", "svd_streaming"):
+        y = ttg.matvec_round(A, x, _mixed(ttg, eps=1e-10, method=ttg.round_method[method]))
+        _close(y, O.matvec_round(A, x, 1e-10, method=method), MIXED_TOL)
+
+
+def test_round_tt_matrix(ttg):
+    # round(tt_matrix) via pack/unpack (round/tt_matrix_round.hpp:27-72)
+    A = O.random_matrix([2, 3, 2, 3], [3, 2, 3, 2], 3, 0xA1)
+    B = O.random_matrix([2, 3, 2, 3], [3, 2, 3, 2], 3, 0xB2)
+    S = O.add(A, B)
+    y = ttg.round(S, ttg.RoundOptions(eps=1e-10))
+    assert y[0].ndim == 4 and y[0].shape[1:3] == (2, 3)
+    _close(y, O.round(S, 1e-10))
