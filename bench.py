@@ -341,9 +341,12 @@ def single_inputs(T, workload):
     if workload == "round_d40":
         a = T.random([8] * 40, 128, 46, fan_in_scale=True)
         b = T.random([8] * 40, 128, 47, fan_in_scale=True)
-        return {"tt": T.add(T.add(a, b), T.ones([8] * 40)), "eps": 1e-8,
+        # ones() gets the same 1/sqrt(r n) core scaling as the random terms;
+        # unscaled, its norm 8^20 would swamp a + b and the sum rounds to rank 1.
+        ones = [c / (8.0 ** 0.5) for c in T.ones([8] * 40)]
+        return {"tt": T.add(T.add(a, b), ones), "eps": 1e-8,
                 "desc": "round(a+b+ones): d=40, n=8, a,b random rank 128 (seeds 46/47), "
-                        "interior rank 257, eps=1e-8"}
+                        "ones scaled 1/sqrt(8) per core, interior rank 257, eps=1e-8"}
     if workload == "matvec_d20":
         A = T.random_matrix([4] * 20, [4] * 20, 8, 44, fan_in_scale=True)
         x = T.random([4] * 20, 32, 45, fan_in_scale=True)

@@ -18,7 +18,7 @@ ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
 SOURCES = ["ttg_kernels.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu"]
-HEADERS = ["ttg_device.cuh", "ttg_job.h", "ttg_kernels.h"]
+HEADERS = ["ttg_device.cuh", "ttg_device_df.cuh", "ttg_df64.cuh", "ttg_job.h", "ttg_kernels.h"]
 
 
 def _nvcc() -> str:

@@ -484,9 +484,10 @@ __device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t
 // src stays readable throughout; fbuf may alias A (it is dead before step 3).
 // Returns the FP64 sweep count.
 // ---------------------------------------------------------------------------
+template <class Gemm>
 __device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
                                 int max_sweeps, int* converged, double* nrm, float* fbuf,
-                                double* tmp, CtaShared& sh)
+                                double* tmp, CtaShared& sh, Gemm gemm)
 {
   float* Af = fbuf;
   float* Vf = fbuf + static_cast<int64_t>(m) * n;
@@ -505,12 +506,12 @@ __device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, 
     Vd[t] = static_cast<double>(Vf[t]);
   __syncthreads();
   // P = Vd^T Vd ; P <- (3I - P)/2 ; V2 = Vd P.
-  cta_gemm(n, n, n, View{Vd, n, 1}, View{Vd, 1, n}, P, 1, n, sh);
+  gemm(n, n, n, View{Vd, n, 1}, View{Vd, 1, n}, P, 1, n, sh);
   for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
     P[t] = ((t % n == t / n) ? 1.5 : 0.0) - 0.5 * P[t];
   __syncthreads();
-  cta_gemm(n, n, n, View{Vd, 1, n}, View{P, 1, n}, V2, 1, n, sh);
-  cta_gemm(m, n, n, src, View{V2, 1, n}, A, 1, lda, sh);
+  gemm(n, n, n, View{Vd, 1, n}, View{P, 1, n}, V2, 1, n, sh);
+  gemm(m, n, n, src, View{V2, 1, n}, A, 1, lda, sh);
   if (Vout)
   {
     for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
