@@ -51,7 +51,12 @@ typedef enum ttg_method {
   TTG_METHOD_SVD_STREAMING = 1,
   TTG_METHOD_SVD_NAIVE = 2,
   TTG_METHOD_ALS = 3,
-  TTG_METHOD_DMRG = 4
+  TTG_METHOD_DMRG = 4,
+  /* Not in the reference: randomised sketch rounding sized by per-bond
+   * sketch ranks (round/ttg_round_batch only).  The sketch is accepted when
+   * its projection error is <= eps/2 (checked exactly); the result is then
+   * rounded with the remaining budget, otherwise the exact SVD round runs. */
+  TTG_METHOD_SKETCH = 5
 } ttg_method;
 
 /* round_gauge (round/round.hpp:49-53). */
@@ -74,6 +79,14 @@ typedef struct ttg_round_options {
   int32_t precision;   /* ttg_precision */
   int32_t max_sweeps;  /* Jacobi sweep limit, 0 = default (40) */
   int32_t reserved;
+  /* TTG_METHOD_SKETCH: sketch rank of every bond, TT by TT (sum over the
+   * tensors of d_i - 1 entries); NULL = the input ranks (no compression). */
+  const int32_t* sketch_ranks;
+  uint64_t sketch_seed;
+  /* Optional: per-bond spectrum summary of the exact rounder, 4 doubles per
+   * bond (largest singular value, smallest kept one, chosen rank, number of
+   * singular values), TT by TT as sketch_ranks.  Filled when non-NULL. */
+  double* bond_stats;
 } ttg_round_options;
 
 /* round_result (round/round.hpp:114-119) plus per-call diagnostics. */
@@ -86,6 +99,9 @@ typedef struct ttg_round_result {
   double device_ms;      /* device time of the call's kernels */
   int32_t status;        /* ttg_status of this tensor */
   int32_t jacobi_sweeps; /* largest Jacobi sweep count met */
+  int32_t sketch_state;  /* 0 exact round, 1 sketch accepted, 2 sketch rejected (exact ran) */
+  int32_t reserved;
+  double sketch_rel_err; /* ||X - sketch(X)|| / ||X|| when a sketch ran */
 } ttg_round_result;
 
 /* A TT (cols == NULL) or TT-matrix (rows = m_k, cols = n_k) in host memory.
@@ -223,6 +239,29 @@ int32_t ttg_plan_kernel_ms(ttg_plan* plan, float* ms);
 /* Bytes moved host->device by upload and device->host by download. */
 int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);
 void ttg_plan_destroy(ttg_plan* plan);
+
+/* ---- rank model of the learned-sketch rounding ---------------------------
+ * No reference counterpart.  A 3-layer MLP (in_features -> hidden -> hidden
+ * -> 1, ReLU, FP32) that maps per-bond features to log(rank); trained on the
+ * GPU by these kernels (mean-squared-error gradient + Adam).  All row
+ * buffers (x: rows x in_features row-major, targets/outputs: rows) are
+ * device pointers; parameters (W1|b1|W2|b2|W3|b3, row-major) live on the
+ * device and cross to the host only through get/set_params. */
+typedef struct ttg_mlp ttg_mlp;
+int32_t ttg_mlp_create(int32_t in_features, int32_t hidden, uint64_t seed, ttg_mlp** out);
+void ttg_mlp_destroy(ttg_mlp* m);
+int32_t ttg_mlp_num_params(const ttg_mlp* m);
+int32_t ttg_mlp_get_params(ttg_mlp* m, float* host);
+int32_t ttg_mlp_set_params(ttg_mlp* m, const float* host);
+int32_t ttg_mlp_forward(ttg_mlp* m, const float* x_dev, int32_t rows, float* y_dev, void* stream);
+/* Gradient of the mean squared error at the current parameters (host copy,
+ * same layout as the parameters) and the loss; synchronises `stream`. */
+int32_t ttg_mlp_gradients(ttg_mlp* m, const float* x_dev, const float* t_dev, int32_t rows,
+                          float* grads_host, double* loss_host, void* stream);
+/* One Adam step (beta 0.9/0.999) on the mean squared error. */
+int32_t ttg_mlp_train_step(ttg_mlp* m, const float* x_dev, const float* t_dev, int32_t rows,
+                           float lr, double* loss_host, void* stream);
+int64_t ttg_mlp_kernel_launches(const ttg_mlp* m);
 
 /* ---- rounding without device allocation -------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

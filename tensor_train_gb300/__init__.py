@@ -41,6 +41,7 @@ class round_method(enum.IntEnum):
     svd_naive = 2
     als = 3
     dmrg = 4
+    sketch = 5  # GB300 extension: randomised sketch rounding with exact check + fallback
 
 
 class round_gauge(enum.IntEnum):
@@ -68,6 +69,9 @@ class RoundOptions:
     gauge: round_gauge = round_gauge.none
     precision: precision = precision.fp64
     max_sweeps: int = 0
+    sketch_ranks: object = None   # per-bond sketch ranks, TT by TT (method = sketch)
+    sketch_seed: int = 0
+    bond_stats: object = None     # numpy float64 array (4 per bond) filled by the exact rounder
 
 
 @dataclasses.dataclass
@@ -81,18 +85,23 @@ class RoundResult:
     device_ms: float = 0.0
     status: int = 0
     jacobi_sweeps: int = 0
+    sketch_state: int = 0
+    sketch_rel_err: float = 0.0
 
 
 class _Opts(C.Structure):
     _fields_ = [("eps", C.c_double), ("max_rank", C.c_int32), ("method", C.c_int32),
                 ("gauge", C.c_int32), ("precision", C.c_int32), ("max_sweeps", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("reserved", C.c_int32), ("sketch_ranks", C.POINTER(C.c_int32)),
+                ("sketch_seed", C.c_uint64), ("bond_stats", C.POINTER(C.c_double))]
 
 
 class _Result(C.Structure):
     _fields_ = [("iters_run", C.c_int32), ("converged", C.c_int32), ("final_resid", C.c_double),
                 ("norm", C.c_double), ("delta", C.c_double), ("device_ms", C.c_double),
-                ("status", C.c_int32), ("jacobi_sweeps", C.c_int32)]
+                ("status", C.c_int32), ("jacobi_sweeps", C.c_int32),
+                ("sketch_state", C.c_int32), ("reserved", C.c_int32),
+                ("sketch_rel_err", C.c_double)]
 
 
 class _Tensor(C.Structure):
@@ -225,13 +234,21 @@ def _check(status: int, what: str):
 
 def _opts(o: RoundOptions | None) -> _Opts:
     o = o or RoundOptions()
-    return _Opts(float(o.eps), int(o.max_rank), int(o.method), int(o.gauge), int(o.precision),
-                 int(o.max_sweeps), 0)
+    c = _Opts(float(o.eps), int(o.max_rank), int(o.method), int(o.gauge), int(o.precision),
+              int(o.max_sweeps), 0)
+    if o.sketch_ranks is not None:
+        arr = np.ascontiguousarray(o.sketch_ranks, dtype=np.int32)
+        c._keep_ranks = arr  # keep the buffer alive with the struct
+        c.sketch_ranks = arr.ctypes.data_as(C.POINTER(C.c_int32))
+    c.sketch_seed = int(o.sketch_seed)
+    if o.bond_stats is not None:
+        c.bond_stats = o.bond_stats.ctypes.data_as(C.POINTER(C.c_double))
+    return c
 
 
 def _result(r: _Result) -> RoundResult:
     return RoundResult(r.iters_run, bool(r.converged), r.final_resid, r.norm, r.delta,
-                       r.device_ms, r.status, r.jacobi_sweeps)
+                       r.device_ms, r.status, r.jacobi_sweeps, r.sketch_state, r.sketch_rel_err)
 
 
 def _take(out: _Tensor):

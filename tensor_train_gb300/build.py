@@ -17,7 +17,7 @@ LIB = os.path.join(BUILD, "libttgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
-SOURCES = ["ttg_kernels.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu"]
+SOURCES = ["ttg_kernels.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu", "ttg_mlp.cu"]
 HEADERS = ["ttg_device.cuh", "ttg_device_df.cuh", "ttg_df64.cuh", "ttg_job.h", "ttg_kernels.h"]
 
 

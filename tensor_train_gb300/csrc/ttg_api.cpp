@@ -220,7 +220,9 @@ struct ttg_plan
   std::vector<int> out_tts;        // TT indices returned to the caller
   std::vector<CoreSlot> slots;
   std::vector<TTInfo> tts;
-  std::vector<int32_t> order, a_idx, b_idx, out_idx;
+  std::vector<int32_t> order, a_idx, b_idx, out_idx, sketch;
+  size_t off_sketch = 0, off_stats = 0;
+  std::vector<BondStat> stats_host;
   int64_t arena_doubles = 0;
   int64_t scratch_stride = 0;
   int grid = 1;
@@ -367,11 +369,15 @@ int32_t layout_and_alloc(ttg_plan& P)
   o = align256(o + sizeof(int32_t) * P.b_idx.size());
   P.off_oidx = o;
   o = align256(o + sizeof(int32_t) * P.out_idx.size());
+  P.off_sketch = o;
+  o = align256(o + sizeof(int32_t) * P.sketch.size());
   P.prefix_bytes = o;
   P.off_pristine = o;
   o = align256(o + P.prefix_bytes);
   P.off_queue = o;
   o = align256(o + 256);
+  P.off_stats = o;
+  o = align256(o + (P.opts.bond_stats ? sizeof(BondStat) * P.slots.size() : 0));
   P.off_scratch = o;
   o = align256(o + sizeof(double) * static_cast<size_t>(P.scratch_stride) * P.grid);
   P.total_bytes = o;
@@ -396,6 +402,8 @@ int32_t layout_and_alloc(ttg_plan& P)
   std::memcpy(h + P.off_slots, P.slots.data(), sizeof(CoreSlot) * P.slots.size());
   std::memcpy(h + P.off_tts, P.tts.data(), sizeof(TTInfo) * P.tts.size());
   std::memcpy(h + P.off_order, P.order.data(), sizeof(int32_t) * P.order.size());
+  if (!P.sketch.empty())
+    std::memcpy(h + P.off_sketch, P.sketch.data(), sizeof(int32_t) * P.sketch.size());
   if (!P.a_idx.empty())
   {
     std::memcpy(h + P.off_aidx, P.a_idx.data(), sizeof(int32_t) * P.a_idx.size());
@@ -428,6 +436,11 @@ RoundJob make_job(ttg_plan& P)
   j.a_idx = reinterpret_cast<const int32_t*>(d + P.off_aidx);
   j.b_idx = reinterpret_cast<const int32_t*>(d + P.off_bidx);
   j.out_idx = reinterpret_cast<const int32_t*>(d + P.off_oidx);
+  j.sketch_ranks = P.sketch.empty() ? nullptr : reinterpret_cast<const int32_t*>(d + P.off_sketch);
+  j.sketch_seed = P.opts.sketch_seed;
+  j.pristine_arena = reinterpret_cast<const double*>(d + P.off_pristine + P.off_arena);
+  j.pristine_slots = reinterpret_cast<const CoreSlot*>(d + P.off_pristine + P.off_slots);
+  j.bond_stats = P.opts.bond_stats ? reinterpret_cast<BondStat*>(d + P.off_stats) : nullptr;
   return j;
 }
 
@@ -445,7 +458,7 @@ int32_t check_opts(const ttg_round_options* o, const char* op)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown precision");
   if (o->method == TTG_METHOD_ALS || o->method == TTG_METHOD_DMRG)
     return fail(TTG_ERR_METHOD, std::string(op) + ": als/dmrg rounding is not served here");
-  if (o->method < 0 || o->method > TTG_METHOD_DMRG)
+  if (o->method < 0 || o->method > TTG_METHOD_SKETCH)
     return fail(TTG_ERR_METHOD, std::string(op) + ": unknown method " + std::to_string(o->method));
   return TTG_OK;
 }
@@ -461,13 +474,17 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
 {
   if (int32_t st = check_opts(opts, op))
     return st;
-  if (opts->method != TTG_METHOD_SVD)
+  if (opts->method != TTG_METHOD_SVD && opts->method != TTG_METHOD_SKETCH)
     return fail(TTG_ERR_METHOD, std::string(op) +
                                     ": round_method::svd_streaming / svd_naive are only valid on "
                                     "matvec_round / matmat_round respectively.");
+  const bool sketch = opts->method == TTG_METHOD_SKETCH;
+  if (sketch && opts->gauge != TTG_GAUGE_NONE)
+    return fail(TTG_ERR_ARG, std::string(op) + ": the sketch method serves gauge none only");
   P.opts = *opts;
   P.kind = kPlanRound;
-  P.job_kind = opts->gauge == TTG_GAUGE_RIGHT_CANONICAL ? kJobRoundRight : kJobRound;
+  P.job_kind = sketch ? kJobRoundSketch
+                      : (opts->gauge == TTG_GAUGE_RIGHT_CANONICAL ? kJobRoundRight : kJobRound);
   P.shapes.resize(static_cast<size_t>(count));
   int64_t need = 64;
   std::vector<std::pair<double, int>> cost;
@@ -476,10 +493,39 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
     if (int32_t st = describe(&ins[i], op, P.shapes[i]))
       return st;
     add_tensor(P, P.shapes[i], true, nullptr);
-    need = std::max(need, round_need(P.shapes[i], P.job_kind));
+    need = std::max(need, round_need(P.shapes[i], sketch ? kJobRound : P.job_kind));
     P.out_tts.push_back(i);
     if (P.shapes[i].d > 1)
       cost.emplace_back(est_cost(P.shapes[i]), i);
+  }
+  if (sketch)
+  {
+    // Sketch-rank table indexed by global core (the bond right of the core).
+    P.sketch.assign(P.slots.size(), 1);
+    int64_t pos = 0;
+    for (int i = 0; i < count; ++i)
+    {
+      const Shape& sh = P.shapes[i];
+      int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1;
+      for (int k = 0; k < sh.d; ++k)
+      {
+        rmax = std::max<int64_t>(rmax, std::max(sh.r[k], sh.r[k + 1]));
+        hmax = std::max<int64_t>(hmax, static_cast<int64_t>(sh.r[k]) * sh.mode(k));
+        nmax = std::max<int64_t>(nmax, sh.mode(k));
+        if (k < sh.d - 1)
+        {
+          int l = opts->sketch_ranks ? opts->sketch_ranks[pos + k] : sh.r[k + 1];
+          if (l < 1)
+            return fail(TTG_ERR_ARG, std::string(op) + ": sketch ranks must be >= 1");
+          l = std::min(l, sh.r[k + 1]);
+          P.sketch[P.tts[i].first + k] = l;
+          lsum += static_cast<int64_t>(sh.r[k + 1]) * l;
+          lmax = std::max<int64_t>(lmax, l);
+        }
+      }
+      pos += sh.d > 0 ? sh.d - 1 : 0;
+      need = std::max(need, need_sketch(rmax, lsum, lmax, hmax, nmax) + 64);
+    }
   }
   std::stable_sort(cost.begin(), cost.end(),
                    [](const auto& a, const auto& b) { return a.first > b.first; });
@@ -530,6 +576,8 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
   if (!P.order.empty() && P.job_kind >= 0)
   {
     TTG_CUDA(cudaMemsetAsync(d + P.off_queue, 0, sizeof(int32_t), st));
+    if (P.opts.bond_stats)
+      TTG_CUDA(cudaMemsetAsync(d + P.off_stats, 0, sizeof(BondStat) * P.slots.size(), st));
     TTG_CUDA(cudaEventRecord(P.evk0, st));
     launch_round(make_job(P), P.grid, st);
     TTG_CUDA(cudaEventRecord(P.evk1, st));
@@ -543,7 +591,30 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
 int32_t plan_download_raw(ttg_plan& P, cudaStream_t st)
 {
   TTG_CUDA(cudaMemcpyAsync(P.host.p, P.dev.p, P.off_order, cudaMemcpyDeviceToHost, st));
+  if (P.opts.bond_stats && !P.slots.empty())
+  {
+    P.stats_host.resize(P.slots.size());
+    TTG_CUDA(cudaMemcpyAsync(P.stats_host.data(), static_cast<char*>(P.dev.p) + P.off_stats,
+                             sizeof(BondStat) * P.slots.size(), cudaMemcpyDeviceToHost, st));
+  }
   TTG_CUDA(cudaStreamSynchronize(st));
+  if (P.opts.bond_stats && !P.slots.empty())
+  {
+    // 4 doubles per bond, TT by TT.
+    int64_t pos = 0;
+    for (size_t t = 0; t < P.tts.size() && t < P.shapes.size(); ++t)
+    {
+      const TTInfo& ti = P.tts[t];
+      for (int k = 0; k + 1 < ti.d; ++k, ++pos)
+      {
+        const BondStat& b = P.stats_host[ti.first + k];
+        P.opts.bond_stats[4 * pos + 0] = b.s_max;
+        P.opts.bond_stats[4 * pos + 1] = b.s_last;
+        P.opts.bond_stats[4 * pos + 2] = b.r_new;
+        P.opts.bond_stats[4 * pos + 3] = b.n_sv;
+      }
+    }
+  }
   return TTG_OK;
 }
 
@@ -604,6 +675,8 @@ void fill_result(const TTInfo& ti, float ms, ttg_round_result* r)
   r->device_ms = ms;
   r->status = ti.status;
   r->jacobi_sweeps = ti.sweeps;
+  r->sketch_state = ti.sketch_state;
+  r->sketch_rel_err = ti.sketch_err;
 }
 
 int32_t first_bad_status(const ttg_plan& P)
@@ -853,7 +926,7 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
     return fail(TTG_ERR_ARG, std::string(op) + ": bad arguments");
   if (int32_t st = check_opts(opts, op))
     return st;
-  if (opts->method != TTG_METHOD_SVD)
+  if (opts->method != TTG_METHOD_SVD && opts->method != TTG_METHOD_SKETCH)
     return fail(TTG_ERR_METHOD, std::string(op) +
                                     ": round_method::svd_streaming / svd_naive are only valid on "
                                     "matvec_round / matmat_round respectively.");
@@ -1110,6 +1183,8 @@ int32_t ttg_matvec_round(const ttg_tensor* A, const ttg_tensor* x, const ttg_rou
     return st;
   if (opts->method == TTG_METHOD_SVD_NAIVE)
     return fail(TTG_ERR_METHOD, "matvec_round: round_method::svd_naive is matmat-only");
+  if (opts->method == TTG_METHOD_SKETCH)
+    return fail(TTG_ERR_METHOD, "matvec_round: the sketch method serves round() only");
   if (opts->gauge != TTG_GAUGE_NONE)
     return fail(TTG_ERR_ARG, "matvec_round: gauge is a round() option");
   const bool streaming = opts->method == TTG_METHOD_SVD_STREAMING && A && A->d > 1;
@@ -1124,6 +1199,8 @@ int32_t ttg_matmat_round(const ttg_tensor* A, const ttg_tensor* B, const ttg_rou
     return st;
   if (opts->method == TTG_METHOD_SVD_STREAMING)
     return fail(TTG_ERR_METHOD, "matmat_round: round_method::svd_streaming is matvec-only");
+  if (opts->method == TTG_METHOD_SKETCH)
+    return fail(TTG_ERR_METHOD, "matmat_round: the sketch method serves round() only");
   if (opts->gauge != TTG_GAUGE_NONE)
     return fail(TTG_ERR_ARG, "matmat_round: gauge is a round() option");
   const bool streaming = opts->method == TTG_METHOD_SVD && A && A->d > 1;

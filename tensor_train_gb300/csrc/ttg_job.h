@@ -81,6 +81,21 @@ struct TTInfo
   int32_t sweeps;  // largest Jacobi sweep count met
   double norm;     // ||T|| computed by the sweep
   double delta;    // truncation threshold used
+  int32_t sketch_state;  // 0 exact round, 1 sketch accepted, 2 sketch rejected -> exact
+  int32_t pad;
+  double sketch_err;     // ||X - Y|| / ||X|| of the sketch projection
+};
+
+// Per-bond record written by the exact rounder when RoundJob::bond_stats is
+// set: the bond's largest singular value, the smallest kept one, the chosen
+// rank and the number of singular values (indexed by the core left of the
+// bond).
+struct BondStat
+{
+  double s_max;
+  double s_last;
+  int32_t r_new;
+  int32_t n_sv;
 };
 
 enum JobKind : int32_t
@@ -90,6 +105,7 @@ enum JobKind : int32_t
   kJobRightOrth = 2,      // right_orthogonalize only
   kJobStreamMatvec = 3,   // build_streaming_matvec (pairs of TTs)
   kJobStreamMatmat = 4,   // build_streaming_matmat
+  kJobRoundSketch = 5,    // randomised sketch rounding with an exact check and fallback
 };
 
 struct RoundJob
@@ -114,6 +130,27 @@ struct RoundJob
   const int32_t* a_idx;
   const int32_t* b_idx;
   const int32_t* out_idx;
+  // Sketch rounding: per core k (< d-1) the sketch rank of the bond to its
+  // right; seed of the Gaussian sketch; the untouched inputs for the exact
+  // fallback (arena and slot table of the pristine copy).
+  const int32_t* sketch_ranks;
+  uint64_t sketch_seed;
+  const double* pristine_arena;
+  const CoreSlot* pristine_slots;
+  BondStat* bond_stats;  // optional per-bond spectrum summary of the exact rounder
 };
+
+// Scratch of the sketch phase of one TT (inner-product chain, stored right
+// environments, one L->R sketch step); the deterministic round that follows
+// uses the ordinary round need.  rmax = largest bond rank, lsum = sum over
+// bonds of r_k * l_k, lmax = largest sketch rank, hmax = largest r_k * n_k,
+// nmax = largest mode.
+TTG_HD inline int64_t need_sketch(int64_t rmax, int64_t lsum, int64_t lmax, int64_t hmax,
+                                  int64_t nmax)
+{
+  return 2 * a32(rmax * rmax) + a32(rmax * nmax * rmax) + a32(lsum) + a32(lmax * nmax * lmax) +
+         a32(hmax * lmax) + 3 * a32(hmax * lmax) + a32(lmax) + a32(lmax * lmax) +
+         a32(lmax * rmax) + a32(lmax * nmax * rmax) + 64 * 8;
+}
 
 }  // namespace ttg

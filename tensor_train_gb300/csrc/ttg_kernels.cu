@@ -125,9 +125,20 @@ __device__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* 
 // Branches as the reference: QR-condense when h >= 2c (truncate.hpp:76-85);
 // otherwise decompose X directly -- by columns when h >= c, by rows (the
 // transpose, accumulating V) when h < c.
+__device__ void record_bond(BondStat* bs, const double* sorted, int nsv, int r_new)
+{
+  if (bs && threadIdx.x == 0)
+  {
+    bs->s_max = sorted[0];
+    bs->s_last = sorted[r_new - 1];
+    bs->r_new = r_new;
+    bs->n_sv = nsv;
+  }
+}
+
 __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
                         bool mixed, Bump bump, Smem sm, double** Ut_out, double** F_out,
-                        TTInfo& T, CtaShared& sh)
+                        TTInfo& T, CtaShared& sh, BondStat* bs = nullptr)
 {
   double* sig;
   double* sorted;
@@ -233,6 +244,7 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
       __syncthreads();
       cta_apply_q(W, h, c, h, tau, U, r_new, h);
     }
+    record_bond(bs, sorted, c, r_new);
     if (threadIdx.x == 0)
     {
       if (!finite(sorted[0]))
@@ -292,6 +304,7 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     __syncthreads();
     // F = U^T X.
     gemm_sel(mixed, r_new, c, h, View{U, h, 1}, X, F, c, 1, sh);
+    record_bond(bs, sorted, c, r_new);
     if (threadIdx.x == 0)
     {
       if (!finite(sorted[0]))
@@ -357,6 +370,7 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     const int jj = static_cast<int>(t / c), j = static_cast<int>(t % c);
     F[t] = A[j + static_cast<int64_t>(ord[jj]) * c];
   }
+  record_bond(bs, sorted, h, r_new);
   if (threadIdx.x == 0)
   {
     if (!finite(sorted[0]))
@@ -440,7 +454,8 @@ __device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bum
 
 // svd_step (detail/truncate.hpp:61-99).
 __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& next,
-                         double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh)
+                         double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh,
+                         BondStat* bs = nullptr)
 {
   const int r = cur.r, n = cur.n, c = cur.rp;
   const int h = r * n;
@@ -450,7 +465,7 @@ __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlo
   double* P = bump.take(static_cast<int64_t>(c) * wn);
   double *U, *F;
   const int r_new = left_svd(View{cs, c, 1}, h, c, delta, job.max_rank, job.max_sweeps,
-                             job.mixed != 0, bump, sm, &U, &F, T, sh);
+                             job.mixed != 0, bump, sm, &U, &F, T, sh, bs);
   gemm_sel(job.mixed != 0, r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, P, wn, 1, sh);
   cta_copy(ns, P, static_cast<int64_t>(r_new) * wn);
   cta_copy_to_rowmajor(cs, r_new, View{U, 1, h}, h, r_new);
@@ -597,7 +612,8 @@ __device__ int64_t balance_need(const CoreSlot* S, int d)
   return a32(total + 1);
 }
 
-__device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh)
+__device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh,
+                         double eps)
 {
   TTInfo& T = job.tts[tti];
   const int d = T.d;
@@ -629,7 +645,7 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
       zero_tt(ar, S, d);
       return;
     }
-    const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+    const double delta = eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
     if (threadIdx.x == 0)
       T.delta = delta;
     for (int k = 0; k < d - 1; ++k)
@@ -637,7 +653,8 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
       if (!fits(job, need_svd_step(static_cast<int64_t>(S[k].r) * S[k].n, S[k].rp,
                                    static_cast<int64_t>(S[k + 1].n) * S[k + 1].rp), T))
         return;
-      svd_step(job, ar, S[k], S[k + 1], delta, Bump{scratch}, sm, T, sh);
+      svd_step(job, ar, S[k], S[k + 1], delta, Bump{scratch}, sm, T, sh,
+               job.bond_stats ? job.bond_stats + T.first + k : nullptr);
     }
     if (!fits(job, balance_need(S, d), T))
       return;
@@ -665,7 +682,7 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
     zero_tt(ar, S, d);
     return;
   }
-  const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+  const double delta = eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
   if (threadIdx.x == 0)
     T.delta = delta;
   for (int k = d - 1; k >= 1; --k)
@@ -675,6 +692,192 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
       return;
     svd_step_right(job, ar, S[k], S[k - 1], delta, Bump{scratch}, sm, T, sh);
   }
+}
+
+// ---------------------------------------------------------------------------
+// Randomised sketch rounding ("randomise-then-orthogonalise", Al Daas et al.,
+// SIAM J. Sci. Comput. 2023) with an exact acceptance test.
+//   1. ||X||^2 by the inner-product chain.
+//   2. Right environments W_k (r_k x l_k) of X against a Gaussian TT with
+//      bond ranks l_k (the sketch ranks, e.g. predicted by the rank model).
+//   3. Left-to-right: Z = left_unfold(X_k) W_{k+1}, Q = qr(Z), X_k <- Q,
+//      X_{k+1} <- (Q^T left_unfold(X_k)) right_unfold(X_{k+1}).  The result
+//      Y is an orthogonal projection of X, so ||X - Y||^2 = ||X||^2 - ||Y||^2,
+//      and ||Y|| = ||last core|| (the other cores are left-orthogonal).
+//   4. Accept when ||X - Y|| <= eps/2 ||X||; Y is then rounded exactly with
+//      the remaining budget eps - ||X - Y||/||X||.  Otherwise the inputs are
+//      restored from the pristine copy and rounded exactly (the fallback that
+//      also judges the sketch).
+// The acceptance test resolves ||X - Y||/||X|| down to ~1e-7 (FP64
+// cancellation of the two squared norms): meant for eps >= 1e-6.
+// ---------------------------------------------------------------------------
+__device__ double sketch_gauss(uint64_t seed, uint64_t tti, uint64_t k, uint64_t i)
+{
+  uint64_t z = seed ^ (tti * 0x9E3779B97F4A7C15ull) ^ (k * 0xC2B2AE3D27D4EB4Full) ^
+               (i * 0x165667B19E3779F9ull);
+  auto mix = [](uint64_t x) {
+    x += 0x9E3779B97F4A7C15ull;
+    x = (x ^ (x >> 30)) * 0xBF58476D1CE4E5B9ull;
+    x = (x ^ (x >> 27)) * 0x94D049BB133111EBull;
+    return x ^ (x >> 31);
+  };
+  const uint64_t a = mix(z), b = mix(z ^ 0xD6E8FEB86659FD93ull);
+  const double u1 = (static_cast<double>(a >> 11) + 0.5) * (1.0 / 9007199254740992.0);
+  const double u2 = static_cast<double>(b >> 11) * (1.0 / 9007199254740992.0);
+  return sqrt(-2.0 * log(u1)) * cos(6.283185307179586 * u2);
+}
+
+__device__ int sketch_rank_of(const RoundJob& job, const CoreSlot* S, int first, int k, int d)
+{
+  // bond k+1 (right of core k); clipped to [1, r_{k+1}]
+  if (k >= d - 1)
+    return 1;
+  int l = job.sketch_ranks ? job.sketch_ranks[first + k] : S[k].rp;
+  l = l < 1 ? 1 : l;
+  return l > S[k].rp ? S[k].rp : l;
+}
+
+__device__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
+                                CtaShared& sh)
+{
+  TTInfo& T = job.tts[tti];
+  const int d = T.d;
+  CoreSlot* S = job.slots + T.first;
+  double* ar = job.arena;
+  const bool mixed = job.mixed != 0;
+  if (d <= 1)
+    return;
+  int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1;
+  for (int k = 0; k < d; ++k)
+  {
+    rmax = imax64(rmax, imax64(S[k].r, S[k].rp));
+    hmax = imax64(hmax, static_cast<int64_t>(S[k].r) * S[k].n);
+    nmax = imax64(nmax, S[k].n);
+    if (k < d - 1)
+    {
+      const int l = sketch_rank_of(job, S, T.first, k, d);
+      lsum += static_cast<int64_t>(S[k].rp) * l;
+      lmax = imax64(lmax, l);
+    }
+  }
+  if (!fits(job, need_sketch(rmax, lsum, lmax, hmax, nmax), T))
+    return;
+  Bump bump{scratch};
+  // 1. ||X||^2 (contract_inner_step chain, detail/contract.hpp:155-205).
+  double* E = bump.take(rmax * rmax);
+  double* En = bump.take(rmax * rmax);
+  double* tmp = bump.take(rmax * nmax * rmax);
+  if (threadIdx.x == 0)
+    E[0] = 1.0;
+  __syncthreads();
+  for (int k = 0; k < d; ++k)
+  {
+    const int ra = S[k].r, n = S[k].n, rap = S[k].rp;
+    const double* ca = ar + S[k].off;
+    gemm_sel(mixed, ra, n * rap, ra, View{E, 1, ra}, View{ca, static_cast<int64_t>(n) * rap, 1},
+             tmp, static_cast<int64_t>(n) * rap, 1, sh);
+    gemm_sel(mixed, rap, rap, ra * n, View{tmp, 1, rap}, View{ca, rap, 1}, En, rap, 1, sh);
+    double* t = E;
+    E = En;
+    En = t;
+  }
+  const double nx2 = E[0];
+  __syncthreads();
+  // 2. Right environments, stored for bonds 1..d-1 (wbuf + woff, woff per core).
+  double* wbuf = bump.take(lsum);
+  double* Rk = bump.take(lmax * nmax * lmax);
+  double* T1 = bump.take(hmax * lmax);
+  double* Wnext = nullptr;  // environment of bond k+1 (1x1 identity for bond d)
+  int64_t woff_next = lsum;
+  for (int k = d - 1; k >= 1; --k)
+  {
+    const int r = S[k].r, n = S[k].n, rp = S[k].rp;
+    const int lk = sketch_rank_of(job, S, T.first, k - 1, d);
+    const int lk1 = sketch_rank_of(job, S, T.first, k, d);
+    const int64_t woff = woff_next - static_cast<int64_t>(r) * lk;
+    double* Wk = wbuf + woff;
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(lk) * n * lk1; t += blockDim.x)
+      Rk[t] = sketch_gauss(job.sketch_seed, static_cast<uint64_t>(tti), static_cast<uint64_t>(k),
+                           static_cast<uint64_t>(t));
+    __syncthreads();
+    const double* xk = ar + S[k].off;
+    if (k == d - 1)
+    {
+      // W_d = 1: T1 = left_unfold(X_{d-1}) (r*n x 1).
+      for (int64_t t = threadIdx.x; t < static_cast<int64_t>(r) * n; t += blockDim.x)
+        T1[t] = xk[t];
+      __syncthreads();
+    }
+    else
+    {
+      gemm_sel(mixed, r * n, lk1, rp, View{xk, rp, 1}, View{Wnext, lk1, 1}, T1, lk1, 1, sh);
+    }
+    // W_k (r x lk) = T1_as (r x n*lk1) * right_unfold(R_k)^T (n*lk1 x lk).
+    gemm_sel(mixed, r, lk, n * lk1, View{T1, static_cast<int64_t>(n) * lk1, 1},
+             View{Rk, 1, static_cast<int64_t>(n) * lk1}, Wk, lk, 1, sh);
+    Wnext = Wk;
+    woff_next = woff;
+  }
+  // 3. Left-to-right sketch-and-orthogonalise.
+  Bump step = bump;
+  for (int k = 0; k < d - 1; ++k)
+  {
+    Bump b2 = step;
+    CoreSlot& cur = S[k];
+    CoreSlot& next = S[k + 1];
+    const int r = cur.r, n = cur.n, rp = cur.rp;
+    const int h = r * n;
+    const int l = sketch_rank_of(job, S, T.first, k, d);
+    // W_{k+1}: bond k+1 environment (rp x l), at its stored offset.
+    int64_t off = 0;
+    for (int j = 1; j < k + 1; ++j)
+      off += static_cast<int64_t>(job.pristine_slots[T.first + j].r) *
+             sketch_rank_of(job, job.pristine_slots + T.first, T.first, j - 1, d);
+    const double* Wk1 = wbuf + off;
+    double* Z = b2.take(static_cast<int64_t>(h) * l);
+    gemm_sel(mixed, h, l, rp, View{ar + cur.off, rp, 1}, View{Wk1, l, 1}, Z, 1, h, sh);
+    double* Wq = b2.take(static_cast<int64_t>(h) * l);
+    double* tau = b2.take(l);
+    double* Rq = b2.take(static_cast<int64_t>(l) * l);
+    double* Q;
+    const int lq = qr_factor(View{Z, 1, h}, h, l, Wq, tau, Rq, Smem{nullptr, 0}, &Q, mixed, sh);
+    // M (lq x rp) = Q^T left_unfold(cur).
+    double* M = b2.take(static_cast<int64_t>(lq) * rp);
+    gemm_sel(mixed, lq, rp, h, View{Q, h, 1}, View{ar + cur.off, rp, 1}, M, rp, 1, sh);
+    const int wn = next.n * next.rp;
+    double* P = b2.take(static_cast<int64_t>(lq) * wn);
+    gemm_sel(mixed, lq, wn, rp, View{M, rp, 1}, View{ar + next.off, wn, 1}, P, wn, 1, sh);
+    cta_copy(ar + next.off, P, static_cast<int64_t>(lq) * wn);
+    cta_copy_to_rowmajor(ar + cur.off, lq, View{Q, 1, h}, h, lq);
+    set_ranks(cur, r, lq);
+    set_ranks(next, lq, next.rp);
+    __syncthreads();
+  }
+  const double ny = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
+  const double err2 = nx2 - ny * ny;
+  const double rel = nx2 > 0.0 ? sqrt(fmax(err2, 0.0) / nx2) : 0.0;
+  const bool accept = isfinite(rel) && rel <= 0.5 * job.eps;
+  if (threadIdx.x == 0)
+  {
+    T.sketch_err = rel;
+    T.sketch_state = accept ? 1 : 2;
+  }
+  __syncthreads();
+  if (accept)
+  {
+    round_tt(job, tti, scratch, sm, sh, job.eps - rel);
+    return;
+  }
+  // Fallback: restore the inputs and round exactly.
+  for (int k = 0; k < d; ++k)
+  {
+    const CoreSlot& p = job.pristine_slots[T.first + k];
+    const double* src = job.pristine_arena + p.off;
+    cta_copy(ar + p.off, src, static_cast<int64_t>(p.r) * p.n * p.rp);
+    set_ranks(S[k], p.r, p.rp);
+  }
+  __syncthreads();
+  round_tt(job, tti, scratch, sm, sh, job.eps);
 }
 
 // build_streaming_matvec / build_streaming_matmat
@@ -835,8 +1038,10 @@ __global__ void __launch_bounds__(kThreads) round_kernel(RoundJob job)
       break;
     if (job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat)
       stream_tt(job, job.order[item], scratch, sm, sh);
+    else if (job.kind == kJobRoundSketch)
+      round_sketch_tt(job, job.order[item], scratch, sm, sh);
     else
-      round_tt(job, job.order[item], scratch, sm, sh);
+      round_tt(job, job.order[item], scratch, sm, sh, job.eps);
   }
 }
 

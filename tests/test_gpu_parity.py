@@ -271,3 +271,46 @@ def test_round_tt_matrix(ttg):
     y = ttg.round(S, ttg.RoundOptions(eps=1e-10))
     assert y[0].ndim == 4 and y[0].shape[1:3] == (2, 3)
     _close(y, O.round(S, 1e-10))
+
+
+# -- randomised sketch rounding (round method `sketch`) ----------------------
+def _small_decaying(seed, rho):
+    from tensor_train_gb300.sketch import decaying_tt
+    t, _ = decaying_tt(seed, d=12, n=4, terms=40, rho=rho)
+    return t
+
+
+def test_sketch_round_accepts_and_matches_exact(ttg):
+    eps = 1e-6
+    tts = [_small_decaying(s, rho) for s, rho in ((1, 0.5), (2, 0.6), (3, 0.7))]
+    exact = [O.round(t, eps) for t in tts]
+    # sketch ranks = exact ranks + 8 oversampling, TT by TT
+    ranks = []
+    for e in exact:
+        ranks += [min(r + 8, 40) for r in O.ranks(e)[1:-1]]
+    res = []
+    ys = ttg.round_batch(tts, ttg.RoundOptions(eps=eps, method=ttg.round_method.sketch,
+                                               sketch_ranks=ranks, sketch_seed=7), res)
+    for t, y, e, r in zip(tts, ys, exact, res):
+        assert r.sketch_state == 1, r
+        assert O.rel_err(y, t) <= eps * 1.01
+        assert all(abs(a - b) <= 1 for a, b in zip(O.ranks(y), O.ranks(e)))
+
+
+def test_sketch_round_rejects_and_falls_back(ttg):
+    eps = 1e-6
+    t = _small_decaying(4, 0.9)
+    res = []
+    y = ttg.round_batch([t], ttg.RoundOptions(eps=eps, method=ttg.round_method.sketch,
+                                              sketch_ranks=[2] * (len(t) - 1)), res)[0]
+    assert res[0].sketch_state == 2  # too small a sketch: rejected, exact round ran
+    _close(y, O.round(t, eps))
+
+
+def test_bond_stats_of_exact_round(ttg):
+    t = _small_decaying(5, 0.6)
+    stats = np.zeros(4 * (len(t) - 1))
+    y = ttg.round_batch([t], ttg.RoundOptions(eps=1e-6, bond_stats=stats))[0]
+    s = stats.reshape(-1, 4)
+    assert list(s[:, 2].astype(int)) == O.ranks(y)[1:-1]
+    assert np.all(s[:, 0] >= s[:, 1]) and np.all(s[:, 1] > 0)
