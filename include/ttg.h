@@ -54,8 +54,9 @@ typedef enum ttg_method {
   TTG_METHOD_DMRG = 4,
   /* Not in the reference: randomised sketch rounding sized by per-bond
    * sketch ranks (round/ttg_round_batch only).  The sketch is accepted when
-   * its projection error is <= eps/2 (checked exactly); the result is then
-   * rounded with the remaining budget, otherwise the exact SVD round runs. */
+   * its projection error is <= eps/4 (checked exactly); the result is then
+   * rounded with the remaining budget sqrt(eps^2 - err^2), otherwise the
+   * exact SVD round runs. */
   TTG_METHOD_SKETCH = 5
 } ttg_method;
 

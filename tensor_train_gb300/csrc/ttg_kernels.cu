@@ -621,7 +621,9 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
   double* ar = job.arena;
   if (d <= 1)
     return;
-  if (job.kind == kJobRound || job.kind == kJobRightOrth)
+  // gauge none (detail::round) for plain, sketch-finishing and orthogonalise
+  // jobs; round_right_canonical only for kJobRoundRight.
+  if (job.kind != kJobRoundRight)
   {
     for (int k = d - 1; k >= 1; --k)
     {
@@ -704,10 +706,13 @@ __device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
 //      X_{k+1} <- (Q^T left_unfold(X_k)) right_unfold(X_{k+1}).  The result
 //      Y is an orthogonal projection of X, so ||X - Y||^2 = ||X||^2 - ||Y||^2,
 //      and ||Y|| = ||last core|| (the other cores are left-orthogonal).
-//   4. Accept when ||X - Y|| <= eps/2 ||X||; Y is then rounded exactly with
-//      the remaining budget eps - ||X - Y||/||X||.  Otherwise the inputs are
-//      restored from the pristine copy and rounded exactly (the fallback that
-//      also judges the sketch).
+//   4. Accept when ||X - Y|| <= eps/4 ||X||.  The final round of Y stays in
+//      the range of the projection, so the two errors are orthogonal:
+//      ||X - round(Y)||^2 = ||X - Y||^2 + ||Y - round(Y)||^2; Y is rounded
+//      with eps_r = sqrt(eps^2 - rel^2) ||X|| / ||Y||, which keeps the total
+//      within eps ||X|| and the per-bond threshold within 3% of the exact
+//      rounder's.  Otherwise the inputs are restored from the pristine copy
+//      and rounded exactly (the fallback that also judges the sketch).
 // The acceptance test resolves ||X - Y||/||X|| down to ~1e-7 (FP64
 // cancellation of the two squared norms): meant for eps >= 1e-6.
 // ---------------------------------------------------------------------------
@@ -856,7 +861,7 @@ __device__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, S
   const double ny = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
   const double err2 = nx2 - ny * ny;
   const double rel = nx2 > 0.0 ? sqrt(fmax(err2, 0.0) / nx2) : 0.0;
-  const bool accept = isfinite(rel) && rel <= 0.5 * job.eps;
+  const bool accept = isfinite(rel) && rel <= 0.25 * job.eps;
   if (threadIdx.x == 0)
   {
     T.sketch_err = rel;
@@ -865,7 +870,9 @@ __device__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, S
   __syncthreads();
   if (accept)
   {
-    round_tt(job, tti, scratch, sm, sh, job.eps - rel);
+    const double eps_r =
+      ny > 0.0 ? sqrt(fmax(job.eps * job.eps - rel * rel, 0.0)) * sqrt(nx2) / ny : job.eps;
+    round_tt(job, tti, scratch, sm, sh, eps_r);
     return;
   }
   // Fallback: restore the inputs and round exactly.

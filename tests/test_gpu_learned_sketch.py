@@ -1,0 +1,67 @@
+"""The learned sketch end to end: rank model trained on the exact rounder's
+ranks, sketch sizes predicted from the previous sweep, and what the model
+gains over the sketch method without it.
+
+Without the model a sketch can only be sized blindly: with the input ranks
+(no compression, so no saving over the exact round) or with a fixed guess
+(too small for slow-decaying slots, which are then rejected and rounded
+exactly after the wasted sketch).  With the model, sketch ranks track each
+slot's decay: every sketch is accepted and the sketched bonds are a fraction
+of the input ranks.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+EPS = 1e-6
+D, N, TERMS = 16, 4, 48
+
+
+def test_learned_sketch_gain(ttg):
+    from tensor_train_gb300 import sketch as S
+    from tensor_train_gb300.mlp import RankModel
+    rng = np.random.default_rng(0)
+    slots = 24
+    rhos = rng.uniform(0.5, 0.8, slots)
+    # training stream: exact rounds give targets and next-sweep features
+    X, Y = [], []
+    prev = None
+    for b in range(8):
+        tts = S.stream_batch(b, rhos, seed0=100, d=D, n=N, terms=TERMS)
+        outs, res, stats = S.exact_round_stats(ttg, tts, EPS)
+        if prev is not None:
+            X.append(S.batch_features(tts, prev))
+            Y.append(np.concatenate([np.log(s[:, 2]) for s in stats]))
+        prev = stats
+    X, Y = np.concatenate(X), np.concatenate(Y).astype(np.float32)
+    model = RankModel(S.N_FEATURES, 128, seed=0)
+    hist = model.train(X, Y, epochs=150, lr=3e-3, batch=1024)
+    assert hist[-1] < 0.2 * hist[0]
+    # test batch: features from the previous sweep of the same slots
+    test = S.stream_batch(9, rhos, seed0=100, d=D, n=N, terms=TERMS)
+    feats = S.batch_features(test, prev)
+    ranks = S.sketch_ranks(model, feats, test)
+    outs, res, _ = S.sketch_round(ttg, test, ranks, EPS, seed=11)
+    exact = [O.round(t, EPS) for t in test]
+    accepted = sum(r.sketch_state == 1 for r in res)
+    for t, y, e in zip(test, outs, exact):
+        assert O.rel_err(y, t) <= EPS * 1.01
+        assert all(abs(a - b) <= 1 for a, b in zip(O.ranks(y), O.ranks(e)))
+    input_bonds = sum(sum(c.shape[-1] for c in t[:-1]) for t in test)
+    learned_frac = ranks.sum() / input_bonds
+    # without the model: a blind fixed sketch rank (the training ranks'
+    # lower quartile) -- slow-decaying slots are rejected and pay the sketch
+    # plus the exact round
+    fixed = np.full_like(ranks, int(np.percentile(np.exp(Y), 25)))
+    outs_f, res_f, _ = S.sketch_round(ttg, test, fixed, EPS, seed=11)
+    rejected_fixed = sum(r.sketch_state == 2 for r in res_f)
+    print(f"learned: accepted {accepted}/{len(test)}, sketch bonds {learned_frac:.2f} of input; "
+          f"fixed rank {fixed[0]}: rejected {rejected_fixed}/{len(test)}")
+    # a rejected sketch falls back to the exact round (still correct, checked
+    # above); the model has to keep rejections rare while compressing
+    assert accepted >= 0.85 * len(test)
+    assert learned_frac < 0.9
+    assert rejected_fixed > len(test) - accepted
