@@ -45,7 +45,8 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="batch",
-                    choices=["batch", "round_d10", "matvec_d20", "round_d40", "eval_d32"],
+                    choices=["batch", "round_d10", "matvec_d20", "round_d40", "eval_d32",
+                             "sketch_d64"],
                     help="batch = the headline (4096 uneven TTs); the others are the single-"
                          "tensor configurations, measured one JSON line each")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
@@ -467,10 +468,115 @@ def run_single(args):
     print(json.dumps(line), flush=True)
 
 
+def run_sketch(args):
+    """Learned-sketch rounding: d=64, n=4, interior rank 200 TTs whose bond
+    spectra decay at rate rho ~ U[0.5, 0.95] per slot, eps=1e-6.  The rank
+    model is trained on the exact rounder's ranks over a stream of the same
+    family (smaller interior ranks, ~50k bonds); the test batch's sketch ranks
+    come from the previous sweep of the same slots.  Reports the learned
+    sketch against the exact rounder (mixed and plain FP64) on the same batch."""
+    import numpy as np
+    import torch
+
+    import tensor_train_gb300 as T
+    from tensor_train_gb300 import sketch as S
+    from tensor_train_gb300.mlp import RankModel
+
+    torch.cuda.set_device(0)
+    eps, d, n = 1e-6, 64, 4
+    slots = args.count if args.count != 4096 else 64
+    rng = np.random.default_rng(2024)
+    rhos = rng.uniform(0.5, 0.95, slots)
+    t0 = time.perf_counter()
+    # training stream: 8 batches, ranks 48..128, exact rounds give targets
+    X, Y, prev = [], [], None
+    train_terms = rng.choice([48, 64, 96, 128], slots)
+    for b in range(8):
+        tts = S.stream_batch(b, rhos, seed0=40000, d=d, n=n, terms=train_terms)
+        _, _, stats = S.exact_round_stats(T, tts, eps)
+        if prev is not None:
+            X.append(S.batch_features(tts, prev))
+            Y.append(np.concatenate([np.log(st[:, 2]) for st in stats]))
+        prev = stats
+    X, Y = np.concatenate(X), np.concatenate(Y).astype(np.float32)
+    gen_s = time.perf_counter() - t0
+    model = RankModel(S.N_FEATURES, 128, seed=0)
+    t0 = time.perf_counter()
+    hist = model.train(X, Y, epochs=60, lr=3e-3, batch=4096)
+    train_s = time.perf_counter() - t0
+    # test stream at full size: sweep 0 exact (features), sweep 1 measured
+    warm = S.stream_batch(100, rhos, seed0=90000, d=d, n=n, terms=200)
+    _, _, prev = S.exact_round_stats(T, warm, eps)
+    del warm
+    test = S.stream_batch(101, rhos, seed0=90000, d=d, n=n, terms=200)
+    feats = S.batch_features(test, prev)
+    t0 = time.perf_counter()
+    ranks = S.sketch_ranks(model, feats, test)
+    predict_s = time.perf_counter() - t0
+
+    def timed(opts):
+        plan = T.Plan("round", test, opts=opts)
+        sptr = torch.cuda.current_stream().cuda_stream
+        plan.upload(sptr)
+        for _ in range(args.warmup):
+            plan.run(sptr)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        ev0.record()
+        for _ in range(args.steps):
+            plan.run(sptr)
+        ev1.record()
+        torch.cuda.synchronize()
+        outs = plan.download(sptr)
+        res = plan.results
+        plan.close()
+        return ev0.elapsed_time(ev1) / args.steps, outs, res
+
+    with Clocks(0) as clk:
+        ms_sk, outs_sk, res_sk = timed(T.RoundOptions(eps=eps, method=T.round_method.sketch,
+                                                      sketch_ranks=ranks, sketch_seed=5,
+                                                      precision=T.precision.mixed))
+        ms_ex, outs_ex, _ = timed(T.RoundOptions(eps=eps, precision=T.precision.mixed))
+        ms_64, _, _ = timed(T.RoundOptions(eps=eps, precision=T.precision.fp64))
+    accepted = sum(r.sketch_state == 1 for r in res_sk)
+    rank_dev = max(max(abs(a - b) for a, b in zip(
+        [y[0].shape[0]] + [c.shape[-1] for c in y], [e[0].shape[0]] + [c.shape[-1] for c in e]))
+        for y, e in zip(outs_sk, outs_ex))
+    line = {"workload": "sketch_d64", "metric": METRIC, "unit": "roundings/s",
+            "config": {"workload": f"learned-sketch rounding: {slots} TTs d=64 n=4 interior rank "
+                                   "200, rho~U[0.5,0.95] per slot, eps=1e-6"},
+            "value": slots / (ms_sk / 1e3), "ms_per_step": ms_sk,
+            "exact_mixed": {"value": slots / (ms_ex / 1e3), "ms_per_step": ms_ex},
+            "exact_plain_fp64": {"value": slots / (ms_64 / 1e3), "ms_per_step": ms_64},
+            "speedup_vs_exact_mixed": ms_ex / ms_sk, "speedup_vs_plain_fp64": ms_64 / ms_sk,
+            "sketch_accepted": f"{accepted}/{slots}",
+            "sketch_bonds_fraction_of_input": float(ranks.sum() /
+                                                     sum(sum(c.shape[-1] for c in t[:-1])
+                                                         for t in test)),
+            "max_rank_deviation_vs_exact": int(rank_dev),
+            "training": {"bonds": int(X.shape[0]), "data_s": gen_s, "train_s": train_s,
+                         "loss_first": hist[0], "loss_last": hist[-1], "predict_s": predict_s,
+                         "mlp_kernel_launches": model.kernel_launches()},
+            "clocks": clk.summary()}
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+        t0 = time.perf_counter()
+        ref = O.round(test[0], eps)
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / sec, "unit": "roundings/s", "cores": 1,
+                                "kind": "port", "sample": "one TT of the batch, oracle exact round"}
+        line["parity"] = {"rel_err_sketch_vs_oracle": O.rel_err(outs_sk[0], ref),
+                          "ranks_within_1": all(abs(a - b) <= 1 for a, b in
+                                                zip(O.ranks(outs_sk[0]), O.ranks(ref)))}
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "sketch_d64":
+        run_sketch(args)
     elif args.workload != "batch":
         run_single(args)
     else:

@@ -243,8 +243,11 @@ void ttg_plan_destroy(ttg_plan* plan);
 
 /* ---- rank model of the learned-sketch rounding ---------------------------
  * No reference counterpart.  A 3-layer MLP (in_features -> hidden -> hidden
- * -> 1, ReLU, FP32) that maps per-bond features to log(rank); trained on the
- * GPU by these kernels (mean-squared-error gradient + Adam).  All row
+ * -> 1, ReLU, FP32 parameters and activations, GEMMs on the tensor cores
+ * with split-BF16 operands as in ttg_tc_gemm_f32) that maps per-bond
+ * features to log(rank); trained on the GPU by these kernels
+ * (mean-squared-error gradient + Adam).  forward, gradients and train_step
+ * synchronise `stream`.  All row
  * buffers (x: rows x in_features row-major, targets/outputs: rows) are
  * device pointers; parameters (W1|b1|W2|b2|W3|b3, row-major) live on the
  * device and cross to the host only through get/set_params. */
@@ -263,6 +266,20 @@ int32_t ttg_mlp_gradients(ttg_mlp* m, const float* x_dev, const float* t_dev, in
 int32_t ttg_mlp_train_step(ttg_mlp* m, const float* x_dev, const float* t_dev, int32_t rows,
                            float lr, double* loss_host, void* stream);
 int64_t ttg_mlp_kernel_launches(const ttg_mlp* m);
+
+/* ---- tensor-core GEMM ---------------------------------------------------
+ * No counterpart in the reference (its GEMMs are Eigen products, e.g.
+ * detail/contract.hpp:50).  C (M x N, row-major, ldc) = A (M x K) * B (K x N)
+ * on the tcgen05 tensor cores, FP32 in and out, FP32 accumulation in TMEM.
+ * A(i, p) = A[i*a_rs + p*a_cs], B(p, j) = B[p*b_rs + j*b_cs]; all device
+ * pointers.  splits = 1: operands rounded to BF16; splits = 3: each operand
+ * split into BF16 hi + lo and the tile accumulates hi*hi + hi*lo + lo*hi
+ * (~1e-5 relative).  The rank model's forward and backward GEMMs use this
+ * kernel.  Synchronises `stream`; TTG_ERR_TIMEOUT if an MMA completion wait
+ * gave up. */
+int32_t ttg_tc_gemm_f32(int32_t M, int32_t N, int32_t K, const float* A, int64_t a_rs,
+                        int64_t a_cs, const float* B, int64_t b_rs, int64_t b_cs, float* C,
+                        int64_t ldc, int32_t splits, void* stream);
 
 /* ---- rounding without device allocation -------------------------------
  * No counterpart in the reference.  For callers that cannot allocate device

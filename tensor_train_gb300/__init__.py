@@ -164,6 +164,9 @@ def lib():
         "ttg_host_axpby": (C.c_int32, [C.c_double, T, C.c_double, T, T]),
         "ttg_host_last_error": (C.c_char_p, []),
         "ttg_device_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+        "ttg_tc_gemm_f32": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
+                                        C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
+                                        C.c_int64, C.c_int32, C.c_void_p]),
     }
     for name, (res, args) in sigs.items():
         f = getattr(L, name)
@@ -515,3 +518,24 @@ def device_fp64_peak() -> float:
     v = C.c_double()
     _check(lib().ttg_device_fp64_peak(C.byref(v)), "device_fp64_peak")
     return v.value
+
+
+def tc_gemm(a, b, splits: int = 3, stream=None):
+    """C = a @ b on the tcgen05 tensor cores (ttg_tc_gemm_f32).
+
+    `a` (M x K) and `b` (K x N) are float32 CUDA tensors with any strides;
+    returns a new contiguous float32 tensor.  splits=3: split-BF16 products
+    (~1e-5 relative); splits=1: plain BF16."""
+    import torch
+    if a.dtype != torch.float32 or b.dtype != torch.float32 or not (a.is_cuda and b.is_cuda):
+        raise TypeError("tc_gemm: float32 CUDA tensors expected")
+    if a.dim() != 2 or b.dim() != 2 or a.shape[1] != b.shape[0]:
+        raise ValueError("tc_gemm: shapes do not chain")
+    M, K = a.shape
+    N = b.shape[1]
+    c = torch.empty((M, N), dtype=torch.float32, device=a.device)
+    st = stream if stream is not None else torch.cuda.current_stream(a.device).cuda_stream
+    _check(lib().ttg_tc_gemm_f32(M, N, K, a.data_ptr(), a.stride(0), a.stride(1), b.data_ptr(),
+                                 b.stride(0), b.stride(1), c.data_ptr(), N, splits, st),
+           "tc_gemm")
+    return c

@@ -1,6 +1,6 @@
 """Compile libttgpu.so (sm_103a) in-tree with nvcc.
 
-Two translation units compiled in parallel, one -gencode, no cmake.
+Translation units compiled in parallel, one -gencode, no cmake.
 """
 from __future__ import annotations
 
@@ -17,8 +17,10 @@ LIB = os.path.join(BUILD, "libttgpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 
-SOURCES = ["ttg_kernels.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu", "ttg_mlp.cu"]
-HEADERS = ["ttg_device.cuh", "ttg_device_df.cuh", "ttg_df64.cuh", "ttg_job.h", "ttg_kernels.h"]
+SOURCES = ["ttg_kernels.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu", "ttg_mlp.cu",
+           "ttg_tc_gemm.cu"]
+HEADERS = ["ttg_device.cuh", "ttg_device_df.cuh", "ttg_df64.cuh", "ttg_job.h", "ttg_kernels.h",
+           "ttg_tc.cuh"]
 
 
 def _nvcc() -> str:

@@ -20,6 +20,12 @@ void launch_inner(const double* ar, const CoreSlot* SA, const CoreSlot* SB, int 
 cudaError_t eval_smem_optin(int rcap);
 cudaError_t round_smem_optin(int smem_doubles);
 void launch_fp64_peak(double* out, int iters, int grid, int block, cudaStream_t stream);
+// tcgen05 split-BF16 GEMM (ttg_tc_gemm.cu): C = A B (+ bias) (relu) (+ C).
+cudaError_t tc_gemm_f32(cudaStream_t st, int M, int N, int K, const float* A, int64_t a_rs,
+                        int64_t a_cs, const float* B, int64_t b_rs, int64_t b_cs, float* C,
+                        int64_t ldc, const float* bias, bool relu, bool accumulate, int splits);
+// Reads and clears the tensor-core GEMM timeout flag (synchronises st).
+bool tc_gemm_timed_out(cudaStream_t st);
 // Sets the message returned by ttg_last_error() on this thread.
 void set_last_error(const std::string& msg);
 

@@ -2,7 +2,8 @@
 //   y = W3^T relu(W2^T relu(W1^T x + b1) + b2) + b3,   x in R^F, hidden H,
 // trained on the GPU with these kernels (forward, backward, Adam).  Rows
 // are bonds, features per bond come from tensor_train_gb300/sketch.py, the
-// target is log(exact rank) from the exact rounder.  FP32 throughout.
+// target is log(exact rank) from the exact rounder.  FP32 parameters and
+// activations; the GEMMs run on the tensor cores with split-BF16 operands.
 //
 // Parameter layout (one device array): W1 (F x H) | b1 (H) | W2 (H x H) |
 // b2 (H) | W3 (H) | b3 (1), all row-major.
@@ -23,64 +24,14 @@ namespace ttg
 namespace
 {
 
-constexpr int kTile = 32;
-
-// C(M x N) = op(A) op(B) (+ bias[n]) (relu), FP32.  op via strides:
-// A(i, p) = A[i*ars + p*acs], B(p, j) = B[p*brs + j*bcs].  With `accumulate`
-// C += result.  32x32 tiles, 32x32 threads... (1024 threads / 4 per thread).
-__global__ void gemm_f32_kernel(int M, int N, int K, const float* __restrict__ A, int64_t ars,
-                                int64_t acs, const float* __restrict__ B, int64_t brs, int64_t bcs,
-                                float* __restrict__ C, int64_t ldc, const float* __restrict__ bias,
-                                int relu, int accumulate)
-{
-  __shared__ float As[kTile][kTile + 1];
-  __shared__ float Bs[kTile][kTile + 1];
-  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads, 4 rows each
-  const int i0 = blockIdx.y * kTile, j0 = blockIdx.x * kTile;
-  float acc[4] = {0.f, 0.f, 0.f, 0.f};
-  for (int p0 = 0; p0 < K; p0 += kTile)
-  {
-    for (int r = ty; r < kTile; r += 8)
-    {
-      const int gi = i0 + r, gp = p0 + tx;
-      As[r][tx] = (gi < M && gp < K) ? A[gi * ars + gp * acs] : 0.f;
-      const int gpb = p0 + r, gj = j0 + tx;
-      Bs[r][tx] = (gpb < K && gj < N) ? B[gpb * brs + gj * bcs] : 0.f;
-    }
-    __syncthreads();
-#pragma unroll 8
-    for (int kk = 0; kk < kTile; ++kk)
-    {
-      const float b = Bs[kk][tx];
-#pragma unroll
-      for (int q = 0; q < 4; ++q)
-        acc[q] = fmaf(As[ty + 8 * q][kk], b, acc[q]);
-    }
-    __syncthreads();
-  }
-#pragma unroll
-  for (int q = 0; q < 4; ++q)
-  {
-    const int gi = i0 + ty + 8 * q, gj = j0 + tx;
-    if (gi < M && gj < N)
-    {
-      float v = acc[q] + (bias ? bias[gj] : 0.f);
-      if (relu)
-        v = fmaxf(v, 0.f);
-      if (accumulate)
-        v += C[gi * ldc + gj];
-      C[gi * ldc + gj] = v;
-    }
-  }
-}
-
+// C(M x N) = op(A) op(B) (+ bias[n]) (relu), FP32 in and out, on the tcgen05
+// tensor cores with split-BF16 operands (ttg_tc_gemm.cu).  op via strides:
+// A(i, p) = A[i*ars + p*acs], B(p, j) = B[p*brs + j*bcs].
 void gemm_f32(cudaStream_t st, int M, int N, int K, const float* A, int64_t ars, int64_t acs,
               const float* B, int64_t brs, int64_t bcs, float* C, int64_t ldc, const float* bias,
               bool relu)
 {
-  dim3 grid((N + kTile - 1) / kTile, (M + kTile - 1) / kTile);
-  gemm_f32_kernel<<<grid, 256, 0, st>>>(M, N, K, A, ars, acs, B, brs, bcs, C, ldc, bias, relu ? 1 : 0,
-                                        0);
+  tc_gemm_f32(st, M, N, K, A, ars, acs, B, brs, bcs, C, ldc, bias, relu, false, 3);
 }
 
 // dy = 2 (y - t) / N; loss partial sums.
@@ -316,6 +267,8 @@ int32_t ttg_mlp_forward(ttg_mlp* m, const float* x_dev, int32_t rows, float* y_d
     return st;
   forward(m, x_dev, rows, y_dev, static_cast<cudaStream_t>(stream));
   MLP_CUDA(cudaGetLastError());
+  if (tc_gemm_timed_out(static_cast<cudaStream_t>(stream)))
+    return mfail(TTG_ERR_TIMEOUT, "mlp: a tensor-core MMA wait timed out");
   return TTG_OK;
 }
 
@@ -350,6 +303,8 @@ static int32_t mlp_backward(ttg_mlp* m, const float* x, const float* t, int rows
   MLP_CUDA(cudaGetLastError());
   MLP_CUDA(cudaMemcpyAsync(loss_host, m->loss, sizeof(double), cudaMemcpyDeviceToHost, st));
   MLP_CUDA(cudaStreamSynchronize(st));
+  if (tc_gemm_timed_out(st))
+    return mfail(TTG_ERR_TIMEOUT, "mlp: a tensor-core MMA wait timed out");
   return TTG_OK;
 }
 
