@@ -15,6 +15,9 @@ namespace ttg
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
+// FP64 Jacobi stops after a sweep whose largest relative rotation is below
+// this (the following sweep's would be ~1e-20).
+constexpr double kJacobiStopRel = 1e-10;
 
 // Column-major / row-major strided view: element (i, j) at p[i*rs + j*cs].
 struct View
@@ -35,6 +38,7 @@ struct CtaShared
   double gemm_a[16][64 + 1];
   double gemm_b[16][64 + 1];
   int flag;
+  unsigned int relbits;  // float bits of a sweep's largest relative rotation
   int item;
   int ival[4];
   double dval[4];
@@ -241,118 +245,6 @@ __device__ void cta_apply_q(const double* A, int m, int kref, int64_t lda, const
   }
 }
 
-// ---------------------------------------------------------------------------
-// One-sided Jacobi (Hestenes) SVD, in place.  A column-major (m x n, lda):
-// on return its columns are mutually orthogonal (A_final = U * diag(s)).
-// V column-major (n x n, ldv) accumulates the rotations when non-null (it
-// must hold the identity, or any start matrix, on entry).  Pairs are visited
-// in the round-robin tournament order, n/2 disjoint pairs per round, one
-// warp per pair.  Squared column norms are cached in nrm[n] (recomputed at
-// the start of every sweep, updated after each rotation as
-// alpha' = alpha - t*gamma, beta' = beta + t*gamma), so a pair costs one dot
-// product and one rotation.  Returns the number of sweeps; *converged = 0 if
-// the limit was reached.  Rotation as in Demmel & Veselic (1992), eq. (4.3).
-// ---------------------------------------------------------------------------
-template <class T>
-__device__ int cta_jacobi(T* A, int m, int n, int64_t lda, T* V, int64_t ldv, int max_sweeps,
-                          int* converged, T* nrm, CtaShared& sh)
-{
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int N = n + (n & 1);
-  const int npairs = N / 2;
-  const T tol = sqrt(static_cast<T>(m > 1 ? m : 1)) * Eps<T>::value();
-  int sweep = 0;
-  *converged = 0;
-  if (n < 2)
-  {
-    *converged = 1;
-    return 0;
-  }
-  for (; sweep < max_sweeps; ++sweep)
-  {
-    __syncthreads();
-    if (threadIdx.x == 0)
-      sh.flag = 0;
-    for (int j = w; j < n; j += kWarps)
-    {
-      const T* a = A + j * lda;
-      T s = 0;
-      for (int i = lane; i < m; i += 32)
-        s += a[i] * a[i];
-      s = warp_sum(s);
-      if (lane == 0)
-        nrm[j] = s;
-    }
-    __syncthreads();
-    for (int r = 0; r < N - 1; ++r)
-    {
-      for (int t = w; t < npairs; t += kWarps)
-      {
-        int p = (t == 0) ? 0 : ((t - 1 + r) % (N - 1)) + 1;
-        int q = ((N - 2 - t + r) % (N - 1)) + 1;
-        if (p >= n || q >= n)
-          continue;
-        if (p > q)
-        {
-          const int tmp = p;
-          p = q;
-          q = tmp;
-        }
-        T* ap = A + p * lda;
-        T* aq = A + q * lda;
-        const T al = nrm[p], be = nrm[q];
-        T ga = 0;
-        for (int i = lane; i < m; i += 32)
-          ga += ap[i] * aq[i];
-        ga = warp_sum(ga);
-        if (ga == T(0) || fabs(ga) <= tol * sqrt(fmax(al, T(0)) * fmax(be, T(0))))
-          continue;
-        const T zeta = (be - al) / (T(2) * ga);
-        T tt;
-        if (fabs(zeta) > T(1.0e18))
-          tt = T(0.5) / zeta;
-        else
-          tt = (zeta >= T(0) ? T(1) : T(-1)) / (fabs(zeta) + sqrt(T(1) + zeta * zeta));
-        const T c = T(1) / sqrt(T(1) + tt * tt);
-        const T s = c * tt;
-        for (int i = lane; i < m; i += 32)
-        {
-          const T x = ap[i], y = aq[i];
-          ap[i] = c * x - s * y;
-          aq[i] = s * x + c * y;
-        }
-        if (V)
-        {
-          T* vp = V + p * ldv;
-          T* vq = V + q * ldv;
-          for (int i = lane; i < n; i += 32)
-          {
-            const T x = vp[i], y = vq[i];
-            vp[i] = c * x - s * y;
-            vq[i] = s * x + c * y;
-          }
-        }
-        if (lane == 0)
-        {
-          nrm[p] = al - tt * ga;
-          nrm[q] = be + tt * ga;
-          sh.flag = 1;
-        }
-      }
-      __syncthreads();
-    }
-    const int any = sh.flag;
-    __syncthreads();
-    if (!any)
-    {
-      *converged = 1;
-      ++sweep;
-      break;
-    }
-  }
-  __syncthreads();
-  return sweep;
-}
 
 // Column norms of A (m x n column-major) into sig[n].
 __device__ void cta_col_norms(const double* A, int m, int n, int64_t lda, double* sig)
@@ -469,56 +361,6 @@ __device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t
         }
     }
   __syncthreads();
-}
-
-// ---------------------------------------------------------------------------
-// Mixed-precision one-sided Jacobi: the sweeps that do most of the rotating
-// run in FP32, one FP64 refinement restores FP64 accuracy.
-//   1. FP32 copy of src (m x n, m >= n) and V32 = I in fbuf
-//      (m*n + n*n floats); FP32 Jacobi sweeps accumulate V32.
-//   2. V = V32 * (3I - V32^T V32)/2 in FP64 (one Newton-Schulz step: V is
-//      orthogonal to FP64 accuracy), in tmp (3 n*n doubles).
-//   3. A = src * V (FP64 GEMM) -- nearly orthogonal columns.
-//   4. FP64 Jacobi sweeps on A (typically one rotating sweep and one check);
-//      when Vout is given it starts from V and accumulates the rotations.
-// src stays readable throughout; fbuf may alias A (it is dead before step 3).
-// Returns the FP64 sweep count.
-// ---------------------------------------------------------------------------
-template <class Gemm>
-__device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
-                                int max_sweeps, int* converged, double* nrm, float* fbuf,
-                                double* tmp, CtaShared& sh, Gemm gemm)
-{
-  float* Af = fbuf;
-  float* Vf = fbuf + static_cast<int64_t>(m) * n;
-  const int64_t mn = static_cast<int64_t>(m) * n, nn = static_cast<int64_t>(n) * n;
-  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
-    Af[t] = static_cast<float>(src(t % m, t / m));
-  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-    Vf[t] = (t % n == t / n) ? 1.0f : 0.0f;
-  __syncthreads();
-  int conv32 = 0;
-  cta_jacobi<float>(Af, m, n, m, Vf, n, 24, &conv32, reinterpret_cast<float*>(nrm), sh);
-  double* Vd = tmp;
-  double* P = tmp + nn;
-  double* V2 = tmp + 2 * nn;
-  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-    Vd[t] = static_cast<double>(Vf[t]);
-  __syncthreads();
-  // P = Vd^T Vd ; P <- (3I - P)/2 ; V2 = Vd P.
-  gemm(n, n, n, View{Vd, n, 1}, View{Vd, 1, n}, P, 1, n, sh);
-  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-    P[t] = ((t % n == t / n) ? 1.5 : 0.0) - 0.5 * P[t];
-  __syncthreads();
-  gemm(n, n, n, View{Vd, 1, n}, View{P, 1, n}, V2, 1, n, sh);
-  gemm(m, n, n, src, View{V2, 1, n}, A, 1, lda, sh);
-  if (Vout)
-  {
-    for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-      Vout[t] = V2[t];
-    __syncthreads();
-  }
-  return cta_jacobi<double>(A, m, n, lda, Vout, n, max_sweeps, converged, nrm, sh);
 }
 
 }  // namespace ttg

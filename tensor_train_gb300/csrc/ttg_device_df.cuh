@@ -215,6 +215,333 @@ __device__ void cta_apply_q_df(const df64* A, int m, int kref, int64_t lda, cons
   }
 }
 
+// Element arithmetic of the one-sided Jacobi below, for FP32, FP64 and df64
+// matrices.  S is the type of the cached squared norms and the rotation
+// parameters (FP64 for df64), Acc the dot-product accumulator.
+template <class E>
+struct JOps;
+template <>
+struct JOps<float>
+{
+  using S = float;
+  using Acc = float;
+  struct Rot
+  {
+    float c, s;
+  };
+  static __device__ __forceinline__ Acc zero() { return 0.0f; }
+  static __device__ __forceinline__ Acc fma(float a, float b, Acc c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
+  static __device__ __forceinline__ Acc shfl(Acc v, int o)
+  {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  static __device__ __forceinline__ S to_s(Acc v) { return v; }
+  static __device__ __forceinline__ S eps() { return 4.0f * FLT_EPSILON; }
+  static __device__ __forceinline__ Rot rot(S c, S s) { return Rot{c, s}; }
+  static __device__ __forceinline__ void apply(const Rot& r, float& x, float& y)
+  {
+    const float a = x, b = y;
+    x = r.c * a - r.s * b;
+    y = r.s * a + r.c * b;
+  }
+};
+template <>
+struct JOps<double>
+{
+  using S = double;
+  using Acc = double;
+  struct Rot
+  {
+    double c, s;
+  };
+  static __device__ __forceinline__ Acc zero() { return 0.0; }
+  static __device__ __forceinline__ Acc fma(double a, double b, Acc c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ Acc add(Acc a, Acc b) { return a + b; }
+  static __device__ __forceinline__ Acc shfl(Acc v, int o)
+  {
+    return __shfl_xor_sync(0xffffffffu, v, o);
+  }
+  static __device__ __forceinline__ S to_s(Acc v) { return v; }
+  static __device__ __forceinline__ S eps() { return DBL_EPSILON; }
+  static __device__ __forceinline__ Rot rot(S c, S s) { return Rot{c, s}; }
+  static __device__ __forceinline__ void apply(const Rot& r, double& x, double& y)
+  {
+    const double a = x, b = y;
+    x = r.c * a - r.s * b;
+    y = r.s * a + r.c * b;
+  }
+};
+template <>
+struct JOps<df64>
+{
+  using S = double;
+  using Acc = df64;
+  struct Rot
+  {
+    df64 c, s, ns;
+  };
+  static __device__ __forceinline__ Acc zero() { return df64{0.0f, 0.0f}; }
+  static __device__ __forceinline__ Acc fma(df64 a, df64 b, Acc c) { return df_fma(a, b, c); }
+  static __device__ __forceinline__ Acc add(Acc a, Acc b) { return df_add(a, b); }
+  static __device__ __forceinline__ Acc shfl(Acc v, int o) { return df_shfl_xor(v, o); }
+  static __device__ __forceinline__ S to_s(Acc v) { return df_to(v); }
+  // df64 carries 48 significand bits.
+  static __device__ __forceinline__ S eps() { return 7.2e-15; }
+  static __device__ __forceinline__ Rot rot(S c, S s)
+  {
+    return Rot{df_from(c), df_from(s), df_from(-s)};
+  }
+  static __device__ __forceinline__ void apply(const Rot& r, df64& x, df64& y)
+  {
+    const df64 a = x, b = y;
+    x = df_fma(r.ns, b, df_mul(r.c, a));
+    y = df_fma(r.s, a, df_mul(r.c, b));
+  }
+};
+
+// ---------------------------------------------------------------------------
+// One-sided Jacobi (Hestenes) SVD, in place.  A column-major (m x n, lda):
+// on return its columns are mutually orthogonal (A_final = U * diag(s)).
+// V column-major (n x n, ldv) accumulates the rotations when non-null (it
+// must hold the identity, or any start matrix, on entry).  Pairs are visited
+// in the round-robin tournament order, n/2 disjoint pairs per round, one
+// group of G lanes per pair (G = 8, 16 or 32 by column length: short
+// columns put several pairs in flight per warp, which is what bounds a
+// latency-bound sweep).  Squared column norms are cached in nrm[n] (recomputed at
+// the start of every sweep, updated after each rotation as
+// alpha' = alpha - t*gamma, beta' = beta + t*gamma), so a pair costs one dot
+// product and one rotation.  Returns the number of sweeps; *converged = 0 if
+// the limit was reached.  Rotation as in Demmel & Veselic (1992), eq. (4.3).
+// ---------------------------------------------------------------------------
+//
+// floor2: a column whose squared norm is <= floor2 is never rotated.  Such
+// columns lie far below the truncation threshold (the caller picks floor2
+// so that all of them together hold a negligible share of delta^2): leaving
+// them out moves the kept singular values and vectors by O(their norm^2),
+// and on rank-deficient inputs they would otherwise keep the sweeps going.
+// (Freezing only pairs of tiny columns is not enough: a column just above
+// the floor never becomes orthogonal to a mutually non-orthogonal frozen
+// set, and the sweeps would cycle.)
+// stop_rel > 0: a sweep whose largest rotated |a_p . a_q| / (|a_p| |a_q|)
+// is below stop_rel ends the iteration (one-sided Jacobi converges
+// quadratically, so the next sweep's rotations would be ~stop_rel^2).
+template <class E>
+__device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, int max_sweeps,
+                          int* converged, typename JOps<E>::S* nrm, CtaShared& sh,
+                          typename JOps<E>::S floor2 = 0, typename JOps<E>::S stop_rel = 0)
+{
+  using O = JOps<E>;
+  using S = typename O::S;
+  using Acc = typename O::Acc;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int G = m <= 128 ? 8 : (m <= 512 ? 16 : 32);
+  const int gpw = 32 / G, ngroups = kWarps * gpw;
+  const int grp = w * gpw + lane / G, gl = lane & (G - 1);
+  const int N = n + (n & 1);
+  const int npairs = N / 2;
+  const S tol = sqrt(static_cast<S>(m > 1 ? m : 1)) * O::eps();
+  auto group_sum = [G](Acc v) {
+    for (int o = G >> 1; o > 0; o >>= 1)
+      v = O::add(v, O::shfl(v, o));
+    return v;
+  };
+  int sweep = 0;
+  *converged = 0;
+  if (n < 2)
+  {
+    *converged = 1;
+    return 0;
+  }
+  for (; sweep < max_sweeps; ++sweep)
+  {
+    __syncthreads();
+    if (threadIdx.x == 0)
+    {
+      sh.flag = 0;
+      sh.relbits = 0u;
+    }
+    for (int j0 = 0; j0 < n; j0 += ngroups)
+    {
+      const int j = j0 + grp;
+      Acc acc = O::zero();
+      if (j < n)
+      {
+        const E* a = A + j * lda;
+        for (int i = gl; i < m; i += G)
+          acc = O::fma(a[i], a[i], acc);
+      }
+      acc = group_sum(acc);
+      if (j < n && gl == 0)
+        nrm[j] = O::to_s(acc);
+    }
+    __syncthreads();
+    for (int r = 0; r < N - 1; ++r)
+    {
+      for (int t0 = 0; t0 < npairs; t0 += ngroups)
+      {
+        const int t = t0 + grp;
+        int p = 0, q = 0;
+        bool act = t < npairs;
+        if (act)
+        {
+          p = (t == 0) ? 0 : ((t - 1 + r) % (N - 1)) + 1;
+          q = ((N - 2 - t + r) % (N - 1)) + 1;
+          if (p >= n || q >= n)
+            act = false;
+          else if (p > q)
+          {
+            const int tmp = p;
+            p = q;
+            q = tmp;
+          }
+        }
+        S al = 0, be = 0;
+        if (act)
+        {
+          al = nrm[p];
+          be = nrm[q];
+          if (al <= floor2 || be <= floor2)
+            act = false;
+        }
+        E* ap = A + p * lda;
+        E* aq = A + q * lda;
+        Acc acc = O::zero();
+        if (act)
+          for (int i = gl; i < m; i += G)
+            acc = O::fma(ap[i], aq[i], acc);
+        acc = group_sum(acc);
+        const S ga = O::to_s(acc);
+        if (!act || ga == S(0) || fabs(ga) <= tol * sqrt(fmax(al, S(0)) * fmax(be, S(0))))
+          continue;
+        const S zeta = (be - al) / (S(2) * ga);
+        S tt;
+        if (fabs(zeta) > S(1.0e18))
+          tt = S(0.5) / zeta;
+        else
+          tt = (zeta >= S(0) ? S(1) : S(-1)) / (fabs(zeta) + sqrt(S(1) + zeta * zeta));
+        const S c = S(1) / sqrt(S(1) + tt * tt);
+        const typename O::Rot R = O::rot(c, c * tt);
+        for (int i = gl; i < m; i += G)
+          O::apply(R, ap[i], aq[i]);
+        if (V)
+        {
+          E* vp = V + p * ldv;
+          E* vq = V + q * ldv;
+          for (int i = gl; i < n; i += G)
+            O::apply(R, vp[i], vq[i]);
+        }
+        if (gl == 0)
+        {
+          nrm[p] = al - tt * ga;
+          nrm[q] = be + tt * ga;
+          sh.flag = 1;
+          const float rel =
+            static_cast<float>(fabs(ga) / sqrt(fmax(al, S(0)) * fmax(be, S(0))));
+          atomicMax(&sh.relbits, __float_as_uint(rel));
+        }
+      }
+      __syncthreads();
+    }
+    const int any = sh.flag;
+    const float maxrel = __uint_as_float(sh.relbits);
+    __syncthreads();
+    if (!any || (stop_rel > S(0) && maxrel < static_cast<float>(stop_rel)))
+    {
+      *converged = 1;
+      ++sweep;
+      break;
+    }
+  }
+  __syncthreads();
+  return sweep;
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision one-sided Jacobi: the sweeps that do most of the rotating
+// run in FP32, a df64 refinement restores FP64-level accuracy.
+//   1. FP32 copy of src (m x n, m >= n) and V32 = I in fbuf
+//      (m*n + n*n floats); FP32 Jacobi sweeps accumulate V32.
+//   2. V = V32 * (3I - V32^T V32)/2 in FP64 (one Newton-Schulz step: V is
+//      orthogonal to FP64 accuracy), in tmp (3 n*n doubles).
+//   3. A = src * V (FP64 GEMM) -- nearly orthogonal columns.
+//   4. df64 Jacobi sweeps on A (typically one or two: the first rotates by
+//      ~1e-7, the next by ~1e-14 and stops the iteration); when Vout is given
+//      it starts from V and accumulates the rotations.
+// src stays readable throughout; fbuf may alias A (it is dead before step 3).
+// Returns the df64 sweep count.
+// ---------------------------------------------------------------------------
+template <class Gemm>
+__device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
+                                int max_sweeps, int* converged, double* nrm, float* fbuf,
+                                double* tmp, CtaShared& sh, Gemm gemm, double floor2 = 0.0)
+{
+  float* Af = fbuf;
+  float* Vf = fbuf + static_cast<int64_t>(m) * n;
+  const int64_t mn = static_cast<int64_t>(m) * n, nn = static_cast<int64_t>(n) * n;
+  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
+    Af[t] = static_cast<float>(src(t % m, t / m));
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    Vf[t] = (t % n == t / n) ? 1.0f : 0.0f;
+  __syncthreads();
+  // FP32 sweeps leave alone columns below ~1e-6 of the RMS column norm
+  // (FP32 cannot resolve them; the high-precision sweeps do) and stop once the
+  // rotations are ~3e-4 (the next sweep would reach FP32 resolution).
+  float ss = 0.f;
+  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
+    ss += Af[t] * Af[t];
+  ss = cta_sum(ss, sh);
+  const float floor32 = fmaxf(static_cast<float>(floor2), 1e-12f * ss / static_cast<float>(n));
+  int conv32 = 0;
+  cta_jacobi<float>(Af, m, n, m, Vf, n, 24, &conv32, reinterpret_cast<float*>(nrm), sh, floor32,
+                    3e-4f);
+  double* Vd = tmp;
+  double* P = tmp + nn;
+  double* V2 = tmp + 2 * nn;
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    Vd[t] = static_cast<double>(Vf[t]);
+  __syncthreads();
+  // P = Vd^T Vd ; P <- (3I - P)/2 ; V2 = Vd P.
+  gemm(n, n, n, View{Vd, n, 1}, View{Vd, 1, n}, P, 1, n, sh);
+  for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+    P[t] = ((t % n == t / n) ? 1.5 : 0.0) - 0.5 * P[t];
+  __syncthreads();
+  gemm(n, n, n, View{Vd, 1, n}, View{P, 1, n}, V2, 1, n, sh);
+  gemm(m, n, n, src, View{V2, 1, n}, A, 1, lda, sh);
+  if (Vout)
+  {
+    for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+      Vout[t] = V2[t];
+    __syncthreads();
+  }
+  // 4. Polish in df64: A / 2^e split once, df64 sweeps, back to FP64.
+  const double sc = cta_pow2_of_max(View{A, 1, lda}, m, n, sh);
+  const double isc = 1.0 / sc;
+  df64* Ad = reinterpret_cast<df64*>(A);
+  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
+  {
+    const int64_t e = (t % m) + (t / m) * lda;
+    Ad[e] = df_from(A[e] * isc);
+  }
+  df64* Vdd = reinterpret_cast<df64*>(Vout);
+  if (Vout)
+    for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+      Vdd[t] = df_from(Vout[t]);
+  __syncthreads();
+  const int sweeps = cta_jacobi<df64>(Ad, m, n, lda, Vdd, n, max_sweeps, converged, nrm, sh,
+                                      floor2 * isc * isc, kJacobiStopRel);
+  for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
+  {
+    const int64_t e = (t % m) + (t / m) * lda;
+    A[e] = df_to(Ad[e]) * sc;
+  }
+  if (Vout)
+    for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
+      Vout[t] = df_to(Vdd[t]);
+  __syncthreads();
+  return sweeps;
+}
+
 // C(i, j) = sum_p A(i, p) B(p, j) in df64 (FP64 in, FP64 out).  A and B are
 // scaled by powers of two (exact) so the split never leaves FP32 range.
 // 64x64 output tiles, 16-deep k slabs in shared memory (the df64 slabs reuse

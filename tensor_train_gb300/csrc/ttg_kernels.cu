@@ -146,6 +146,10 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
   double* U;
   double* F;
   int sweeps = 0, conv = 1;
+  // Columns below this squared norm hold < 1e-6 delta^2 all together, so
+  // they always land in the truncated tail: Jacobi does not rotate them.
+  const int nsv = h < c ? h : c;
+  const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
   if (h >= 2 * c)
   {
     double* W = bump.take(static_cast<int64_t>(h) * c);
@@ -192,14 +196,15 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
       float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(cc));
       double* tmp = bump.take(3 * cc);
       sweeps = cta_jacobi_mixed(View{R, 1, c}, c, c, A, c, nullptr, max_sweeps, &conv, nrm, fbuf,
-                                tmp, sh, GemmDf{});
+                                tmp, sh, GemmDf{}, floor2);
     }
     else
     {
       for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
         A[t] = R[t];
       __syncthreads();
-      sweeps = cta_jacobi<double>(A, c, c, c, nullptr, 0, max_sweeps, &conv, nrm, sh);
+      sweeps = cta_jacobi<double>(A, c, c, c, nullptr, 0, max_sweeps, &conv, nrm, sh, floor2,
+                                  kJacobiStopRel);
     }
     cta_col_norms(A, c, c, c, sig);
     cta_argsort_desc(sig, c, ord, sorted);
@@ -281,13 +286,14 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
       float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(hc));
       double* tmp = bump.take(3 * static_cast<int64_t>(c) * c);
       sweeps = cta_jacobi_mixed(X, h, c, A, h, nullptr, max_sweeps, &conv, nrm, fbuf, tmp, sh,
-                                GemmDf{});
+                                GemmDf{}, floor2);
     }
     else
     {
       cta_copy_to_colmajor(A, h, X, h, c);
       __syncthreads();
-      sweeps = cta_jacobi<double>(A, h, c, h, nullptr, 0, max_sweeps, &conv, nrm, sh);
+      sweeps = cta_jacobi<double>(A, h, c, h, nullptr, 0, max_sweeps, &conv, nrm, sh, floor2,
+                                  kJacobiStopRel);
     }
     cta_col_norms(A, h, c, h, sig);
     cta_argsort_desc(sig, c, ord, sorted);
@@ -344,7 +350,7 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(ch));
     double* tmp = bump.take(3 * hh);
     sweeps = cta_jacobi_mixed(transposed(X), c, h, A, c, V, max_sweeps, &conv, nrm, fbuf, tmp, sh,
-                              GemmDf{});
+                              GemmDf{}, floor2);
   }
   else
   {
@@ -352,7 +358,8 @@ __device__ int left_svd(View X, int h, int c, double delta, int max_rank, int ma
     for (int64_t t = threadIdx.x; t < hh; t += blockDim.x)
       V[t] = (t % h == t / h) ? 1.0 : 0.0;
     __syncthreads();
-    sweeps = cta_jacobi<double>(A, c, h, c, V, h, max_sweeps, &conv, nrm, sh);
+    sweeps = cta_jacobi<double>(A, c, h, c, V, h, max_sweeps, &conv, nrm, sh, floor2,
+                                kJacobiStopRel);
   }
   cta_col_norms(A, c, h, c, sig);
   cta_argsort_desc(sig, h, ord, sorted);
