@@ -285,8 +285,10 @@ struct round_options
   std::uint64_t seed = 0;
   const tt* warm_start_tt = nullptr;
   const tt_matrix* warm_start_tt_matrix = nullptr;
-  // GB300 knobs (not in the reference): arithmetic of the bulk contractions.
+  // GB300 knobs (not in the reference): arithmetic of the bulk contractions
+  // and the device schedule (one CTA per TT, or the whole GPU per TT).
   ttg_precision precision = TTG_PREC_FP64;
+  ttg_schedule schedule = TTG_SCHED_AUTO;
 };
 struct round_result
 {
@@ -390,6 +392,7 @@ inline ttg_round_options to_c(const round_options& o)
   c.method = static_cast<int32_t>(o.method);
   c.gauge = static_cast<int32_t>(o.gauge);
   c.precision = o.precision;
+  c.schedule = o.schedule;
   return c;
 }
 

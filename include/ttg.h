@@ -70,6 +70,16 @@ typedef enum ttg_gauge { TTG_GAUGE_NONE = 0, TTG_GAUGE_RIGHT_CANONICAL = 1 } ttg
  * values; QR and contractions stay FP64. */
 typedef enum ttg_precision { TTG_PREC_FP64 = 0, TTG_PREC_MIXED = 1 } ttg_precision;
 
+/* Device schedule of a round (gauge none, method svd): one CTA per TT with
+ * many TTs in flight, or the whole GPU on one TT at a time (cooperative
+ * launch; for a few large TTs).  AUTO picks the whole GPU when a call
+ * holds at most 4 TTs with a bond rank of 64 or more. */
+typedef enum ttg_schedule {
+  TTG_SCHED_AUTO = 0,
+  TTG_SCHED_PER_TT = 1,
+  TTG_SCHED_WHOLE_GPU = 2
+} ttg_schedule;
+
 /* round_options (round/round.hpp:55-105), SVD-relevant fields plus the
  * device-side knobs.  Zero-initialise and set what you need. */
 typedef struct ttg_round_options {
@@ -79,7 +89,7 @@ typedef struct ttg_round_options {
   int32_t gauge;       /* ttg_gauge */
   int32_t precision;   /* ttg_precision */
   int32_t max_sweeps;  /* Jacobi sweep limit, 0 = default (40) */
-  int32_t reserved;
+  int32_t schedule;    /* ttg_schedule */
   /* TTG_METHOD_SKETCH: sketch rank of every bond, TT by TT (sum over the
    * tensors of d_i - 1 entries); NULL = the input ranks (no compression). */
   const int32_t* sketch_ranks;

@@ -54,6 +54,13 @@ class precision(enum.IntEnum):
     mixed = 1
 
 
+class schedule(enum.IntEnum):
+    """Device schedule (ttg_schedule): one CTA per TT, or the whole GPU per TT."""
+    auto = 0
+    per_tt = 1
+    whole_gpu = 2
+
+
 class TTGError(RuntimeError):
     def __init__(self, status: int, message: str):
         super().__init__(f"[{status}] {message}")
@@ -69,6 +76,7 @@ class RoundOptions:
     gauge: round_gauge = round_gauge.none
     precision: precision = precision.fp64
     max_sweeps: int = 0
+    schedule: int = 0             # schedule.auto / per_tt / whole_gpu
     sketch_ranks: object = None   # per-bond sketch ranks, TT by TT (method = sketch)
     sketch_seed: int = 0
     bond_stats: object = None     # numpy float64 array (4 per bond) filled by the exact rounder
@@ -92,7 +100,7 @@ class RoundResult:
 class _Opts(C.Structure):
     _fields_ = [("eps", C.c_double), ("max_rank", C.c_int32), ("method", C.c_int32),
                 ("gauge", C.c_int32), ("precision", C.c_int32), ("max_sweeps", C.c_int32),
-                ("reserved", C.c_int32), ("sketch_ranks", C.POINTER(C.c_int32)),
+                ("schedule", C.c_int32), ("sketch_ranks", C.POINTER(C.c_int32)),
                 ("sketch_seed", C.c_uint64), ("bond_stats", C.POINTER(C.c_double))]
 
 
@@ -238,7 +246,7 @@ def _check(status: int, what: str):
 def _opts(o: RoundOptions | None) -> _Opts:
     o = o or RoundOptions()
     c = _Opts(float(o.eps), int(o.max_rank), int(o.method), int(o.gauge), int(o.precision),
-              int(o.max_sweeps), 0)
+              int(o.max_sweeps), int(o.schedule))
     if o.sketch_ranks is not None:
         arr = np.ascontiguousarray(o.sketch_ranks, dtype=np.int32)
         c._keep_ranks = arr  # keep the buffer alive with the struct

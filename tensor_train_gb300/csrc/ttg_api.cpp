@@ -233,6 +233,11 @@ struct ttg_plan
     int a_slot, x_slot, y_slot, r, m, p, rp, s, nout, sp;
   };
   std::vector<Apply> applies;
+  // whole-GPU schedule (wide_round_kernel)
+  bool wide = false;
+  int wide_grid = 0;
+  WideJob wjob{};
+  DevMem wdev;
   // byte layout of the device buffer
   size_t off_arena = 0, off_slots = 0, off_tts = 0, off_order = 0, off_aidx = 0, off_bidx = 0,
          off_oidx = 0, prefix_bytes = 0, off_pristine = 0, off_queue = 0, off_scratch = 0,
@@ -347,6 +352,95 @@ double est_cost(const Shape& s)
 constexpr int kSmemTwoPerSm = 11776;  // 92 KB
 constexpr int kSmemOnePerSm = 25600;  // 200 KB
 
+// Whole-GPU schedule: chosen for round jobs (gauge none, method svd) by
+// the options, or automatically for at most 4 TTs with a bond rank >= 64.
+// Work buffers are sized for the largest core and rank of the TTs swept.
+int32_t setup_wide(ttg_plan& P)
+{
+  P.wide = false;
+  if (P.job_kind != kJobRound || P.order.empty() || P.opts.schedule == TTG_SCHED_PER_TT)
+    return TTG_OK;
+  int64_t core_max = 1, c_max = 1, cols_max = 1;
+  for (int t : P.order)
+  {
+    const TTInfo& ti = P.tts[t];
+    int64_t cols = 0;
+    for (int k = 0; k < ti.d; ++k)
+    {
+      const CoreSlot& c = P.slots[ti.first + k];
+      core_max = std::max<int64_t>(core_max, static_cast<int64_t>(c.r) * c.n * c.rp);
+      c_max = std::max<int64_t>(c_max, std::max(c.r, c.rp));
+      cols += c.rp;
+    }
+    cols_max = std::max(cols_max, cols);
+  }
+  const bool want = P.opts.schedule == TTG_SCHED_WHOLE_GPU ||
+                    (P.order.size() <= 4 && c_max >= 64);
+  if (!want)
+    return TTG_OK;
+  // Jacobi block pairs: (2 c_max rows + c_max V rows) x 2b columns + 2b norms.
+  int jb = 4;
+  while (jb > 1 && (6 * c_max + 2) * jb > kSmemOnePerSm)
+    jb /= 2;
+  if ((6 * c_max + 2) * jb > kSmemOnePerSm)
+    return TTG_OK;  // ranks beyond the block buffers: stay per TT
+  const int64_t smem = kSmemOnePerSm;
+  int grid = 0;
+  const cudaError_t e = wide_round_setup(static_cast<int>(smem), &grid);
+  if (e != cudaSuccess)
+    return fail(TTG_ERR_CUDA, std::string("whole-GPU round setup: ") + cudaGetErrorString(e));
+  if (grid < 2)
+    return TTG_OK;
+  const int ms = P.opts.max_sweeps > 0 ? P.opts.max_sweeps : 40;
+  size_t o = 0;
+  auto take = [&](size_t bytes) {
+    const size_t r = o;
+    o = align256(o + bytes);
+    return r;
+  };
+  const size_t cc = sizeof(double) * static_cast<size_t>(c_max * c_max);
+  const size_t cm = sizeof(double) * static_cast<size_t>(core_max);
+  const size_t oW = take(cm), oU = take(cm), oP = take(cm), oA = take(cm), oR = take(cc),
+               oV = take(cc), oF = take(cc), otau = take(8 * c_max), osig = take(8 * c_max),
+               osorted = take(8 * c_max), oord = take(4 * c_max), ocn = take(8 * (cols_max + 1)),
+               oival = take(64), orot = take(4 * ms), orel = take(4 * ms), obar = take(sizeof(GridBar));
+  TTG_CUDA(P.wdev.ensure(o));
+  char* b = static_cast<char*>(P.wdev.p);
+  char* d = static_cast<char*>(P.dev.p);
+  WideJob& j = P.wjob;
+  j = WideJob{};
+  j.arena = reinterpret_cast<double*>(d + P.off_arena);
+  j.slots = reinterpret_cast<CoreSlot*>(d + P.off_slots);
+  j.tts = reinterpret_cast<TTInfo*>(d + P.off_tts);
+  j.order = reinterpret_cast<const int32_t*>(d + P.off_order);
+  j.ntt = static_cast<int32_t>(P.order.size());
+  j.max_rank = P.opts.max_rank;
+  j.max_sweeps = ms;
+  j.jblock = jb;
+  j.smem_doubles = smem;
+  j.eps = P.opts.eps;
+  j.W = reinterpret_cast<double*>(b + oW);
+  j.Ub = reinterpret_cast<double*>(b + oU);
+  j.Pb = reinterpret_cast<double*>(b + oP);
+  j.A = reinterpret_cast<double*>(b + oA);
+  j.R = reinterpret_cast<double*>(b + oR);
+  j.V = reinterpret_cast<double*>(b + oV);
+  j.F = reinterpret_cast<double*>(b + oF);
+  j.tau = reinterpret_cast<double*>(b + otau);
+  j.sig = reinterpret_cast<double*>(b + osig);
+  j.sorted = reinterpret_cast<double*>(b + osorted);
+  j.ord = reinterpret_cast<int*>(b + oord);
+  j.cn = reinterpret_cast<double*>(b + ocn);
+  j.ival = reinterpret_cast<int*>(b + oival);
+  j.sweep_rot = reinterpret_cast<unsigned int*>(b + orot);
+  j.sweep_rel = reinterpret_cast<unsigned int*>(b + orel);
+  j.bar = reinterpret_cast<GridBar*>(b + obar);
+  j.bond_stats = P.opts.bond_stats ? reinterpret_cast<BondStat*>(d + P.off_stats) : nullptr;
+  P.wide = true;
+  P.wide_grid = grid;
+  return TTG_OK;
+}
+
 int32_t layout_and_alloc(ttg_plan& P)
 {
   static const cudaError_t optin = round_smem_optin(kSmemOnePerSm);
@@ -412,7 +506,7 @@ int32_t layout_and_alloc(ttg_plan& P)
   }
   P.h2d = static_cast<int64_t>(P.prefix_bytes);
   P.d2h = static_cast<int64_t>(P.off_order);
-  return TTG_OK;
+  return setup_wide(P);
 }
 
 RoundJob make_job(ttg_plan& P)
@@ -579,7 +673,13 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
     if (P.opts.bond_stats)
       TTG_CUDA(cudaMemsetAsync(d + P.off_stats, 0, sizeof(BondStat) * P.slots.size(), st));
     TTG_CUDA(cudaEventRecord(P.evk0, st));
-    launch_round(make_job(P), P.grid, st);
+    if (P.wide)
+    {
+      TTG_CUDA(cudaMemsetAsync(P.wjob.bar, 0, sizeof(GridBar), st));
+      TTG_CUDA(launch_wide_round(P.wjob, P.wide_grid, st));
+    }
+    else
+      launch_round(make_job(P), P.grid, st);
     TTG_CUDA(cudaEventRecord(P.evk1, st));
     P.kernel_timed = true;
     g_launches += 1;
@@ -597,7 +697,12 @@ int32_t plan_download_raw(ttg_plan& P, cudaStream_t st)
     TTG_CUDA(cudaMemcpyAsync(P.stats_host.data(), static_cast<char*>(P.dev.p) + P.off_stats,
                              sizeof(BondStat) * P.slots.size(), cudaMemcpyDeviceToHost, st));
   }
+  GridBar bar{};
+  if (P.wide)
+    TTG_CUDA(cudaMemcpyAsync(&bar, P.wjob.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, st));
   TTG_CUDA(cudaStreamSynchronize(st));
+  if (P.wide && bar.err)
+    return fail(TTG_ERR_TIMEOUT, "whole-GPU round: a grid barrier wait timed out");
   if (P.opts.bond_stats && !P.slots.empty())
   {
     // 4 doubles per bond, TT by TT.

@@ -309,12 +309,11 @@ __device__ int trunc_rank_serial(const double* s, int n, double delta, int max_r
 // through (c_rs, c_cs).  64x64 output tiles, 16-deep k slabs in shared
 // memory, 4x4 register tile per thread.
 // ---------------------------------------------------------------------------
-__device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
-                         int64_t c_cs, CtaShared& sh)
+// One 64x64 output tile at (i0, j0).
+__device__ void cta_gemm_tile(int i0, int j0, int M, int N, int K, View A, View B, double* C,
+                              int64_t c_rs, int64_t c_cs, CtaShared& sh)
 {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  for (int i0 = 0; i0 < M; i0 += 64)
-    for (int j0 = 0; j0 < N; j0 += 64)
     {
       double acc[4][4];
 #pragma unroll
@@ -360,6 +359,14 @@ __device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t
             C[gi * c_rs + gj * c_cs] = acc[a][b];
         }
     }
+}
+
+__device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
+                         int64_t c_cs, CtaShared& sh)
+{
+  for (int i0 = 0; i0 < M; i0 += 64)
+    for (int j0 = 0; j0 < N; j0 += 64)
+      cta_gemm_tile(i0, j0, M, N, K, A, B, C, c_rs, c_cs, sh);
   __syncthreads();
 }
 

@@ -303,8 +303,9 @@ struct JOps<df64>
 // ---------------------------------------------------------------------------
 // One-sided Jacobi (Hestenes) SVD, in place.  A column-major (m x n, lda):
 // on return its columns are mutually orthogonal (A_final = U * diag(s)).
-// V column-major (n x n, ldv) accumulates the rotations when non-null (it
-// must hold the identity, or any start matrix, on entry).  Pairs are visited
+// V column-major (vrows x n, ldv; vrows = n by default) accumulates the
+// rotations when non-null (it must hold the identity, or any start matrix,
+// on entry).  Pairs are visited
 // in the round-robin tournament order, n/2 disjoint pairs per round, one
 // group of G lanes per pair (G = 8, 16 or 32 by column length: short
 // columns put several pairs in flight per warp, which is what bounds a
@@ -329,7 +330,8 @@ struct JOps<df64>
 template <class E>
 __device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, int max_sweeps,
                           int* converged, typename JOps<E>::S* nrm, CtaShared& sh,
-                          typename JOps<E>::S floor2 = 0, typename JOps<E>::S stop_rel = 0)
+                          typename JOps<E>::S floor2 = 0, typename JOps<E>::S stop_rel = 0,
+                          float* maxrel_out = nullptr, int vrows = -1)
 {
   using O = JOps<E>;
   using S = typename O::S;
@@ -428,7 +430,8 @@ __device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, in
         {
           E* vp = V + p * ldv;
           E* vq = V + q * ldv;
-          for (int i = gl; i < n; i += G)
+          const int vr = vrows < 0 ? n : vrows;
+          for (int i = gl; i < vr; i += G)
             O::apply(R, vp[i], vq[i]);
         }
         if (gl == 0)
@@ -446,6 +449,8 @@ __device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, in
     const int any = sh.flag;
     const float maxrel = __uint_as_float(sh.relbits);
     __syncthreads();
+    if (maxrel_out)
+      *maxrel_out = maxrel;
     if (!any || (stop_rel > S(0) && maxrel < static_cast<float>(stop_rel)))
     {
       *converged = 1;

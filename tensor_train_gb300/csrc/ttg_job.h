@@ -108,6 +108,49 @@ enum JobKind : int32_t
   kJobRoundSketch = 5,    // randomised sketch rounding with an exact check and fallback
 };
 
+// Grid barrier word of the whole-GPU kernel (zeroed before each launch).
+struct GridBar
+{
+  unsigned int count;
+  unsigned int gen;
+  int err;
+  int pad;
+};
+
+// Whole-GPU rounding of a few large TTs (wide_round_kernel): the arena,
+// slots and TT records as in RoundJob, plus grid-shared work buffers sized
+// for the largest core (core_max doubles) and rank (c_max).
+struct WideJob
+{
+  double* arena;
+  CoreSlot* slots;
+  TTInfo* tts;
+  const int* order;
+  int ntt;
+  int max_rank;
+  int max_sweeps;
+  int jblock;          // Jacobi block width (columns)
+  int64_t smem_doubles;
+  double eps;
+  double* W;           // core_max: reflectors
+  double* Ub;          // core_max: U / work columns
+  double* Pb;          // core_max: contraction output
+  double* A;           // core_max: Jacobi matrix
+  double* R;           // c_max^2
+  double* V;           // c_max^2
+  double* F;           // c_max^2
+  double* tau;         // c_max
+  double* sig;         // c_max
+  double* sorted;      // c_max
+  int* ord;            // c_max
+  double* cn;          // sum of ranks: balancing column norms
+  int* ival;           // [0] = truncation rank of the current bond
+  unsigned int* sweep_rot;  // max_sweeps
+  unsigned int* sweep_rel;  // max_sweeps
+  GridBar* bar;
+  BondStat* bond_stats;
+};
+
 struct RoundJob
 {
   double* arena;

@@ -1189,6 +1189,38 @@ __global__ void __launch_bounds__(kThreads) inner_kernel(const double* __restric
     *out = E[0];
 }
 
+#include "ttg_wide.cuh"
+
+cudaError_t launch_wide_round(const WideJob& job, int grid, cudaStream_t stream)
+{
+  WideJob j = job;
+  void* args[] = {&j};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(wide_round_kernel), dim3(grid),
+                                     dim3(kThreads), args,
+                                     sizeof(double) * static_cast<size_t>(job.smem_doubles),
+                                     stream);
+}
+
+cudaError_t wide_round_setup(int smem_doubles, int* max_grid)
+{
+  cudaError_t e = cudaFuncSetAttribute(wide_round_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(double) * smem_doubles));
+  if (e != cudaSuccess)
+    return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+    &per_sm, wide_round_kernel, kThreads, sizeof(double) * static_cast<size_t>(smem_doubles));
+  if (e != cudaSuccess)
+    return e;
+  // One CTA per SM: the phases are latency-bound, more CTAs only add
+  // barrier arrivals.
+  *max_grid = per_sm >= 1 ? sms : 0;
+  return cudaSuccess;
+}
+
 void launch_round(const RoundJob& job, int grid, cudaStream_t stream)
 {
   const size_t smem = sizeof(double) * static_cast<size_t>(job.smem_doubles);

@@ -11,6 +11,10 @@ namespace ttg
 {
 
 void launch_round(const RoundJob& job, int grid, cudaStream_t stream);
+// Whole-GPU rounding (cooperative launch, grid <= the value from setup).
+cudaError_t launch_wide_round(const WideJob& job, int grid, cudaStream_t stream);
+// Opt-in to the dynamic shared memory and the co-resident grid size.
+cudaError_t wide_round_setup(int smem_doubles, int* max_grid);
 void launch_apply_core(const double* A, const double* X, double* Y, int r, int m, int p, int rp,
                        int s, int nout, int sp, cudaStream_t stream);
 void launch_eval(const double* ar, const CoreSlot* S, int d, const int* idx, int64_t M,

@@ -1,0 +1,631 @@
+// Whole-GPU rounding of a few large TTs (part of the sweep translation unit,
+// included by ttg_kernels.cu).
+//
+// One cooperative launch, one CTA per SM; the CTAs work on one TT at a time
+// and meet at a grid barrier between dependent phases.  Same algorithm and
+// branch structure as round_tt (detail::round, round/tt_round.hpp:36-134),
+// each step spread over the grid:
+//   * Householder QR (qr_thin, types/tt_eigen_bridge.hpp:42-60): column l
+//     belongs to CTA l mod P.  The owner of column j forms reflector j and
+//     publishes it; after one barrier every CTA applies it to its own
+//     columns.  Owned columns stay in shared memory when they fit.
+//   * Q and Q [Uc; 0]: each CTA forms its own columns from the published
+//     reflectors -- no barriers.
+//   * One-sided Jacobi SVD: block-pair rounds.  Columns are cut into blocks
+//     of b; in each round of the round-robin tournament over blocks a CTA
+//     loads a block pair into shared memory, runs one local sweep over all
+//     pairs of its 2b columns (cta_jacobi) and writes them back; a barrier
+//     ends the round.  Outer sweeps stop when a sweep rotates nothing or its
+//     largest relative rotation is below kJacobiStopRel.
+//   * Contractions: 64x64 FP64 output tiles spread over the CTAs.
+// Arithmetic is FP64 throughout: with one TT on the whole GPU the sweep is
+// bound by the dependency chain (one reflector, one Jacobi round after the
+// other), not by the FP64 pipes.
+//
+// Every barrier wait is bounded (kGridWaitCycles): a CTA that gives up sets
+// the shared error word, every other CTA sees it at its next barrier, and
+// the kernel returns; the host reports TTG_ERR_TIMEOUT.
+// Included inside namespace ttg.
+#pragma once
+
+constexpr long long kGridWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
+
+// Bounded grid barrier (sense by generation counter).  All CTAs are
+// co-resident (cooperative launch).  Returns false once any CTA timed out.
+__device__ bool grid_sync(GridBar* gb)
+{
+  __shared__ int ok_sh;
+  __syncthreads();
+  if (threadIdx.x == 0)
+  {
+    int ok = 1;
+    volatile unsigned int* genp = &gb->gen;
+    volatile int* errp = &gb->err;
+    const unsigned int g = *genp;
+    __threadfence();
+    if (atomicAdd(&gb->count, 1u) == gridDim.x - 1)
+    {
+      atomicExch(&gb->count, 0u);
+      __threadfence();
+      atomicAdd(&gb->gen, 1u);
+    }
+    else
+    {
+      const long long t0 = clock64();
+      while (*genp == g)
+      {
+        if (*errp)
+          break;
+        if (clock64() - t0 > kGridWaitCycles)
+        {
+          atomicExch(&gb->err, 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*errp)
+      ok = 0;
+    ok_sh = ok;
+  }
+  __syncthreads();
+  return ok_sh != 0;
+}
+
+#define WSYNC()                 \
+  do                            \
+  {                             \
+    if (!grid_sync(job.bar))    \
+      return false;             \
+  } while (0)
+
+struct WideSmem
+{
+  double* p;
+  int64_t cap;  // doubles
+};
+
+// dst[0..n) = src[0..n), spread over the grid.
+__device__ void wide_copy(double* dst, const double* src, int64_t n)
+{
+  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n; t += stride)
+    dst[t] = src[t];
+}
+
+// C = A B over the grid: 64x64 tiles, tile t on CTA t mod P.
+__device__ void wide_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
+                          int64_t c_cs, CtaShared& sh)
+{
+  const int tm = (M + 63) / 64, tn = (N + 63) / 64;
+  for (int t = blockIdx.x; t < tm * tn; t += gridDim.x)
+    cta_gemm_tile((t / tn) * 64, (t % tn) * 64, M, N, K, A, B, C, c_rs, c_cs, sh);
+  __syncthreads();
+}
+
+// Householder QR of X (h x c), column-distributed.  Reflector tails go to
+// job.W (column-major, ld h), scales to job.tau, R (k x c, column-major,
+// ld k) to job.R.  Returns k = min(h, c); false in *ok on a barrier failure.
+__device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, CtaShared& sh,
+                       bool* ok)
+{
+  const int P = gridDim.x, me = blockIdx.x;
+  const int k = h < c ? h : c;
+  const int nown = (c - me + P - 1) / P > 0 ? (c - me + P - 1) / P : 0;
+  const bool in_smem = static_cast<int64_t>(nown) * h <= sm.cap;
+  auto col = [&](int l) -> double* {
+    return in_smem ? sm.p + static_cast<int64_t>(l / P) * h : job.W + static_cast<int64_t>(l) * h;
+  };
+  for (int l = me; l < c; l += P)
+  {
+    double* y = col(l);
+    for (int i = threadIdx.x; i < h; i += blockDim.x)
+      y[i] = X(i, l);
+  }
+  __syncthreads();
+  for (int j = 0; j < k; ++j)
+  {
+    const int len = h - j;
+    if (j % P == me)
+    {
+      double* x = col(j) + j;
+      double part = 0.0;
+      for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
+        part += x[i] * x[i];
+      const double tail2 = cta_sum(part, sh);
+      const double x0 = x[0];
+      double beta, t, inv;
+      if (tail2 <= DBL_MIN)
+      {
+        t = 0.0;
+        beta = x0;
+        inv = 0.0;
+      }
+      else
+      {
+        beta = sqrt(x0 * x0 + tail2);
+        if (x0 >= 0.0)
+          beta = -beta;
+        inv = 1.0 / (x0 - beta);
+        t = (beta - x0) / beta;
+      }
+      double* pub = job.W + static_cast<int64_t>(j) * h + j;
+      for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
+      {
+        x[i] *= inv;
+        pub[i] = x[i];
+      }
+      if (threadIdx.x == 0)
+      {
+        x[0] = beta;
+        pub[0] = beta;
+        job.tau[j] = t;
+      }
+    }
+    if (!grid_sync(job.bar))
+    {
+      *ok = false;
+      return k;
+    }
+    const double t = job.tau[j];
+    if (t == 0.0)
+      continue;
+    const double* v = job.W + static_cast<int64_t>(j) * h + j;
+    for (int l = me; l < c; l += P)
+    {
+      if (l <= j)
+        continue;
+      double* y = col(l) + j;
+      double part = 0.0;
+      for (int i = threadIdx.x; i < len; i += blockDim.x)
+        part += (i == 0 ? 1.0 : v[i]) * y[i];
+      const double dot = cta_sum(part, sh) * t;
+      for (int i = threadIdx.x; i < len; i += blockDim.x)
+        y[i] -= dot * (i == 0 ? 1.0 : v[i]);
+      __syncthreads();
+    }
+  }
+  // R columns from their owners.
+  for (int l = me; l < c; l += P)
+  {
+    const double* y = col(l);
+    for (int i = threadIdx.x; i < k; i += blockDim.x)
+      job.R[i + static_cast<int64_t>(l) * k] = (i <= l) ? y[i] : 0.0;
+  }
+  if (!grid_sync(job.bar))
+    *ok = false;
+  return k;
+}
+
+// Column l (l mod P == this CTA) of H_0 ... H_{kref-1} [B(:, l); 0] into
+// out(i, l) = out[i*o_rs + l*o_cs], for l < ncols; B column-major (nb x
+// ncols, ld nb), nb <= h.  y is a length-h work column.
+__device__ void wide_apply_q(const WideJob& job, int h, int kref, const double* B, int nb,
+                             int ncols, double* out, int64_t o_rs, int64_t o_cs, bool eye,
+                             WideSmem sm, CtaShared& sh)
+{
+  const int P = gridDim.x, me = blockIdx.x;
+  for (int l = me; l < ncols; l += P)
+  {
+    double* y = (h <= sm.cap) ? sm.p : job.Ub + static_cast<int64_t>(l) * h;
+    for (int i = threadIdx.x; i < h; i += blockDim.x)
+      y[i] = eye ? (i == l ? 1.0 : 0.0) : (i < nb ? B[i + static_cast<int64_t>(l) * nb] : 0.0);
+    __syncthreads();
+    // For the identity start, H_j with j > l leaves e_l unchanged.
+    const int jtop = eye ? (l < kref - 1 ? l : kref - 1) : kref - 1;
+    for (int j = jtop; j >= 0; --j)
+    {
+      const double t = job.tau[j];
+      if (t == 0.0)
+        continue;
+      const double* v = job.W + static_cast<int64_t>(j) * h + j;
+      double* yj = y + j;
+      const int len = h - j;
+      double part = 0.0;
+      for (int i = threadIdx.x; i < len; i += blockDim.x)
+        part += (i == 0 ? 1.0 : v[i]) * yj[i];
+      const double dot = cta_sum(part, sh) * t;
+      for (int i = threadIdx.x; i < len; i += blockDim.x)
+        yj[i] -= dot * (i == 0 ? 1.0 : v[i]);
+      __syncthreads();
+    }
+    for (int i = threadIdx.x; i < h; i += blockDim.x)
+      out[i * o_rs + static_cast<int64_t>(l) * o_cs] = y[i];
+    __syncthreads();
+  }
+}
+
+// One-sided Jacobi of A (p x q, column-major, lda) in block-pair rounds over
+// the grid; V (q x q, ld q) accumulates the rotations when non-null.
+// Returns the outer sweep count; *conv = 0 if max_sweeps was reached.
+__device__ bool wide_jacobi(const WideJob& job, double* A, int p, int q, int64_t lda, double* V,
+                            double floor2, WideSmem sm, CtaShared& sh, int* sweeps_out, int* conv)
+{
+  const int P = gridDim.x, me = blockIdx.x;
+  const int b = job.jblock;
+  const int nblk = (q + b - 1) / b;
+  const int NB = nblk + (nblk & 1), npairs = NB / 2;
+  double* As = sm.p;
+  double* Vs = As + static_cast<int64_t>(p) * 2 * b;
+  double* ns = Vs + (V ? static_cast<int64_t>(q) * 2 * b : 0);
+  if (me == 0)
+    for (int s = threadIdx.x; s < job.max_sweeps; s += blockDim.x)
+    {
+      job.sweep_rot[s] = 0u;
+      job.sweep_rel[s] = 0u;
+    }
+  WSYNC();
+  *conv = 0;
+  *sweeps_out = job.max_sweeps;
+  if (q < 2)
+  {
+    *conv = 1;
+    *sweeps_out = 0;
+    return true;
+  }
+  for (int sw = 0; sw < job.max_sweeps; ++sw)
+  {
+    for (int rr = 0; rr < NB - 1; ++rr)
+    {
+      for (int t = me; t < npairs; t += P)
+      {
+        const int bp = (t == 0) ? 0 : ((t - 1 + rr) % (NB - 1)) + 1;
+        const int bq = ((NB - 2 - t + rr) % (NB - 1)) + 1;
+        const int c0 = bp * b, c1 = bq * b;
+        const int np = c0 < q ? (q - c0 < b ? q - c0 : b) : 0;
+        const int nq = c1 < q ? (q - c1 < b ? q - c1 : b) : 0;
+        const int nc = np + nq;
+        if (nc < 2)
+          continue;
+        auto gcol = [&](int j) { return j < np ? c0 + j : c1 + (j - np); };
+        for (int64_t e = threadIdx.x; e < static_cast<int64_t>(p) * nc; e += blockDim.x)
+        {
+          const int i = static_cast<int>(e % p), j = static_cast<int>(e / p);
+          As[e] = A[i + static_cast<int64_t>(gcol(j)) * lda];
+        }
+        if (V)
+          for (int64_t e = threadIdx.x; e < static_cast<int64_t>(q) * nc; e += blockDim.x)
+          {
+            const int i = static_cast<int>(e % q), j = static_cast<int>(e / q);
+            Vs[e] = V[i + static_cast<int64_t>(gcol(j)) * q];
+          }
+        __syncthreads();
+        int lconv = 1;
+        float mr = 0.0f;
+        cta_jacobi<double>(As, p, nc, p, V ? Vs : nullptr, q, 1, &lconv, ns, sh, floor2, 0.0, &mr,
+                           q);
+        if (!lconv && threadIdx.x == 0)
+        {
+          atomicOr(&job.sweep_rot[sw], 1u);
+          atomicMax(&job.sweep_rel[sw], __float_as_uint(mr));
+        }
+        for (int64_t e = threadIdx.x; e < static_cast<int64_t>(p) * nc; e += blockDim.x)
+        {
+          const int i = static_cast<int>(e % p), j = static_cast<int>(e / p);
+          A[i + static_cast<int64_t>(gcol(j)) * lda] = As[e];
+        }
+        if (V)
+          for (int64_t e = threadIdx.x; e < static_cast<int64_t>(q) * nc; e += blockDim.x)
+          {
+            const int i = static_cast<int>(e % q), j = static_cast<int>(e / q);
+            V[i + static_cast<int64_t>(gcol(j)) * q] = Vs[e];
+          }
+        __syncthreads();
+      }
+      WSYNC();
+    }
+    const unsigned int rot = *reinterpret_cast<volatile unsigned int*>(&job.sweep_rot[sw]);
+    const unsigned int rel = *reinterpret_cast<volatile unsigned int*>(&job.sweep_rel[sw]);
+    if (!rot || __uint_as_float(rel) < static_cast<float>(kJacobiStopRel))
+    {
+      *conv = 1;
+      *sweeps_out = sw + 1;
+      return true;
+    }
+  }
+  return true;
+}
+
+// Singular values = column norms of A (p x q); sorted/ord/r_new by CTA 0.
+// Ends with a barrier; returns false on a barrier failure.
+__device__ bool wide_truncate(const WideJob& job, const double* A, int p, int q, int64_t lda,
+                              double delta, TTInfo& T, BondStat* bs, CtaShared& sh)
+{
+  const int P = gridDim.x, me = blockIdx.x;
+  for (int j = me; j < q; j += P)
+  {
+    const double* a = A + static_cast<int64_t>(j) * lda;
+    double s = 0.0;
+    for (int i = threadIdx.x; i < p; i += blockDim.x)
+      s += a[i] * a[i];
+    s = cta_sum(s, sh);
+    if (threadIdx.x == 0)
+      job.sig[j] = sqrt(s);
+  }
+  WSYNC();
+  if (me == 0)
+  {
+    cta_argsort_desc(job.sig, q, job.ord, job.sorted);
+    if (threadIdx.x == 0)
+    {
+      job.ival[0] = trunc_rank_serial(job.sorted, q, delta, job.max_rank);
+      if (!finite(job.sorted[0]))
+        set_status(T, kStatusNan);
+    }
+    __syncthreads();
+    record_bond(bs, job.sorted, q, job.ival[0]);
+  }
+  WSYNC();
+  return true;
+}
+
+// Norm balancing (round/tt_round.hpp:65-124) over the grid: core k on CTA
+// k mod P for the column norms and for the scaling; every CTA forms the
+// geometric mean from all norms in the same order.
+__device__ bool wide_balance(const WideJob& job, double* ar, CoreSlot* S, int d, CtaShared& sh)
+{
+  const int P = gridDim.x, me = blockIdx.x;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  int64_t base = 0;
+  for (int k = 0; k < d - 1; ++k)
+  {
+    const int h = S[k].r * S[k].n, c = S[k].rp;
+    if (k % P == me)
+    {
+      const double* p = ar + S[k].off;
+      for (int col = w; col < c; col += kWarps)
+      {
+        double s = 0.0;
+        for (int i = lane; i < h; i += 32)
+          s += p[static_cast<int64_t>(i) * c + col] * p[static_cast<int64_t>(i) * c + col];
+        s = warp_sum(s);
+        if (lane == 0)
+          job.cn[base + col] = sqrt(s);
+      }
+    }
+    base += c;
+  }
+  WSYNC();
+  double my_log = 0.0, my_cnt = 0.0;
+  for (int64_t i = threadIdx.x; i < base; i += blockDim.x)
+  {
+    const double nc = job.cn[i];
+    if (nc > 0.0)
+    {
+      my_log += log(nc);
+      my_cnt += 1.0;
+    }
+  }
+  const double tot_log = cta_sum(my_log, sh);
+  const double tot_cnt = cta_sum(my_cnt, sh);
+  if (tot_cnt <= 0.0)
+    return true;
+  const double geo = exp(tot_log / tot_cnt);
+  base = 0;
+  int64_t prev_base = 0;
+  for (int k = 0; k < d; ++k)
+  {
+    const int r = S[k].r, n = S[k].n, c = S[k].rp;
+    if (k % P == me)
+    {
+      double* p = ar + S[k].off;
+      const int64_t sz = static_cast<int64_t>(r) * n * c;
+      for (int64_t t = threadIdx.x; t < sz; t += blockDim.x)
+      {
+        const int a = static_cast<int>(t / (static_cast<int64_t>(n) * c));
+        const int b = static_cast<int>(t % c);
+        double x = p[t];
+        if (k >= 1)
+        {
+          const double nr = job.cn[prev_base + a];
+          if (nr > 0.0)
+            x /= geo / nr;
+        }
+        if (k <= d - 2)
+        {
+          const double nc = job.cn[base + b];
+          if (nc > 0.0)
+            x *= geo / nc;
+        }
+        p[t] = x;
+      }
+    }
+    if (k <= d - 2)
+    {
+      prev_base = base;
+      base += c;
+    }
+  }
+  return true;
+}
+
+// detail::round (gauge none) of TT tti over the whole grid.
+__device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShared& sh)
+{
+  TTInfo& T = job.tts[tti];
+  const int d = T.d;
+  CoreSlot* S = job.slots + T.first;
+  double* ar = job.arena;
+  const int me = blockIdx.x;
+  const bool lead = (me == 0 && threadIdx.x == 0);
+  if (d <= 1)
+    return true;
+  // Right-to-left QR sweep (right_qr_step, detail/orthogonalize.hpp:63-100).
+  for (int k = d - 1; k >= 1; --k)
+  {
+    const int r = S[k].r, n = S[k].n, rp = S[k].rp;
+    const int w = n * rp;
+    const int hp = S[k - 1].r * S[k - 1].n;
+    double* cs = ar + S[k].off;
+    double* ps = ar + S[k - 1].off;
+    bool ok = true;
+    const int kk = wide_qr(job, View{cs, 1, w}, w, r, sm, sh, &ok);
+    if (!ok)
+      return false;
+    // core_k <- Q^T (Q column-major w x kk is the core's row-major layout);
+    // prev (hp x kk) = left_unfold(prev) R^T.
+    wide_apply_q(job, w, kk, nullptr, 0, kk, cs, 1, w, true, sm, sh);
+    wide_gemm(hp, kk, r, View{ps, r, 1}, View{job.R, kk, 1}, job.Pb, kk, 1, sh);
+    WSYNC();
+    wide_copy(ps, job.Pb, static_cast<int64_t>(hp) * kk);
+    if (lead)
+    {
+      set_ranks(S[k], kk, rp);
+      set_ranks(S[k - 1], S[k - 1].r, kk);
+    }
+    WSYNC();
+  }
+  const double nrm = core_norm(ar + S[0].off, core_size(S[0]), sh);
+  if (lead)
+    T.norm = nrm;
+  if (!isfinite(nrm))
+  {
+    if (me == 0)
+      set_status(T, kStatusNan);
+    return true;
+  }
+  if (nrm == 0.0)
+  {
+    if (me == 0)
+      zero_tt(ar, S, d);
+    WSYNC();
+    return true;
+  }
+  const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+  if (lead)
+    T.delta = delta;
+  // Left-to-right truncated SVD sweep (svd_step, detail/truncate.hpp:61-99).
+  for (int k = 0; k < d - 1; ++k)
+  {
+    const int r = S[k].r, n = S[k].n, c = S[k].rp;
+    const int h = r * n;
+    const int wn = S[k + 1].n * S[k + 1].rp;
+    double* cs = ar + S[k].off;
+    double* ns = ar + S[k + 1].off;
+    const View X{cs, c, 1};
+    const int nsv = h < c ? h : c;
+    const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
+    BondStat* bs = job.bond_stats ? job.bond_stats + T.first + k : nullptr;
+    int sweeps = 0, conv = 1, r_new = 1;
+    if (h >= 2 * c)
+    {
+      bool ok = true;
+      wide_qr(job, X, h, c, sm, sh, &ok);
+      if (!ok)
+        return false;
+      // A = R (c x c), then Jacobi.
+      wide_copy(job.A, job.R, static_cast<int64_t>(c) * c);
+      WSYNC();
+      if (!wide_jacobi(job, job.A, c, c, c, nullptr, floor2, sm, sh, &sweeps, &conv))
+        return false;
+      if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
+        return false;
+      r_new = job.ival[0];
+      // Uc (c x r_new) = A(:, ord) / s, into V.
+      for (int j = me; j < r_new; j += gridDim.x)
+      {
+        const double s = job.sorted[j];
+        const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
+        for (int i = threadIdx.x; i < c; i += blockDim.x)
+          job.V[i + static_cast<int64_t>(j) * c] = s > 0.0 ? a[i] / s : 0.0;
+      }
+      WSYNC();
+      // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
+      wide_gemm(r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sh);
+      wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
+      WSYNC();
+    }
+    else if (h >= c)
+    {
+      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+           e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+        job.A[e] = X(e % h, e / h);
+      WSYNC();
+      if (!wide_jacobi(job, job.A, h, c, h, nullptr, floor2, sm, sh, &sweeps, &conv))
+        return false;
+      if (!wide_truncate(job, job.A, h, c, h, delta, T, bs, sh))
+        return false;
+      r_new = job.ival[0];
+      for (int j = me; j < r_new; j += gridDim.x)
+      {
+        const double s = job.sorted[j];
+        const double* a = job.A + static_cast<int64_t>(job.ord[j]) * h;
+        for (int i = threadIdx.x; i < h; i += blockDim.x)
+          job.Ub[i + static_cast<int64_t>(j) * h] = s > 0.0 ? a[i] / s : 0.0;
+      }
+      WSYNC();
+      // F = U^T X.
+      wide_gemm(r_new, c, h, View{job.Ub, h, 1}, X, job.F, c, 1, sh);
+      WSYNC();
+    }
+    else
+    {
+      // Jacobi on X^T (c x h); V (h x h) accumulates and becomes U.
+      const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+           e < static_cast<int64_t>(c) * h; e += stride)
+        job.A[e] = X(e / c, e % c);
+      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+           e < static_cast<int64_t>(h) * h; e += stride)
+        job.V[e] = (e % h == e / h) ? 1.0 : 0.0;
+      WSYNC();
+      if (!wide_jacobi(job, job.A, c, h, c, job.V, floor2, sm, sh, &sweeps, &conv))
+        return false;
+      if (!wide_truncate(job, job.A, c, h, c, delta, T, bs, sh))
+        return false;
+      r_new = job.ival[0];
+      for (int j = me; j < r_new; j += gridDim.x)
+      {
+        const int o = job.ord[j];
+        for (int i = threadIdx.x; i < h; i += blockDim.x)
+          job.Ub[i + static_cast<int64_t>(j) * h] = job.V[i + static_cast<int64_t>(o) * h];
+        for (int i = threadIdx.x; i < c; i += blockDim.x)
+          job.F[static_cast<int64_t>(j) * c + i] = job.A[i + static_cast<int64_t>(o) * c];
+      }
+      WSYNC();
+    }
+    if (lead)
+    {
+      if (!conv)
+        set_status(T, kStatusNotConverged);
+      if (sweeps > T.sweeps)
+        T.sweeps = sweeps;
+    }
+    // next (r_new x wn) = F right_unfold(next); core_k <- U (row-major).
+    wide_gemm(r_new, wn, c, View{job.F, c, 1}, View{ns, wn, 1}, job.Pb, wn, 1, sh);
+    WSYNC();
+    wide_copy(ns, job.Pb, static_cast<int64_t>(r_new) * wn);
+    {
+      const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+           e < static_cast<int64_t>(h) * r_new; e += stride)
+      {
+        const int64_t i = e / r_new, j = e % r_new;
+        cs[e] = job.Ub[i + j * h];
+      }
+    }
+    if (lead)
+    {
+      set_ranks(S[k], r, r_new);
+      set_ranks(S[k + 1], r_new, S[k + 1].rp);
+    }
+    WSYNC();
+  }
+  if (!wide_balance(job, ar, S, d, sh))
+    return false;
+  WSYNC();
+  return true;
+}
+
+__global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
+{
+  extern __shared__ double dyn_smem[];
+  __shared__ CtaShared sh;
+  const WideSmem sm{dyn_smem, job.smem_doubles};
+  for (int i = 0; i < job.ntt; ++i)
+    if (!wide_round_tt(job, job.order ? job.order[i] : i, sm, sh))
+      return;
+}
+
+#undef WSYNC

@@ -1,0 +1,110 @@
+"""Whole-GPU schedule (one TT over all SMs, cooperative launch) against the
+CPU oracle and against the one-CTA-per-TT schedule.
+
+Same tolerances as the parity tests: exact ranks, relative Frobenius error
+1e-11 (FP64 both sides).  The cases cover the three SVD branches of
+svd_step (detail/truncate.hpp:61-99: rows >= 2 cols, cols <= rows < 2 cols,
+rows < cols), the rank shrink of right_qr_step (detail/orthogonalize.hpp:84)
+and a truncating, rank-deficient input.
+"""
+import numpy as np
+import pytest
+
+from oracle import pyoracle as O
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-11
+
+
+def _opts(ttg, eps, sched, **kw):
+    return ttg.RoundOptions(eps=eps, schedule=sched, **kw)
+
+
+def _close(y, yref, tol=TOL):
+    assert O.ranks(y) == O.ranks(yref), (O.ranks(y), O.ranks(yref))
+    err = O.rel_err(y, yref)
+    assert err <= tol, err
+
+
+def test_whole_gpu_config1_rank_shrink(ttg):
+    # add(a, b) with rank 16 where only 4 is feasible: the R->L QR shrinks it
+    a = O.random([4] * 10, 8, 42, fan_in_scale=True)
+    b = O.random([4] * 10, 8, 43, fan_in_scale=True)
+    t = O.add(a, b)
+    info = ttg.RoundResult()
+    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu), info)
+    _close(y, O.round(t, 1e-8))
+    assert info.status == 0 and info.converged
+
+
+def test_whole_gpu_large_random(ttg):
+    # interior rank 65 (two rank-32 terms and ones), n = 4: rows = 4 * 65 >= 2 * 65
+    a = O.random([4] * 8, 32, 7, fan_in_scale=True)
+    b = O.random([4] * 8, 32, 8, fan_in_scale=True)
+    ones = [c / 2.0 for c in O.ones([4] * 8)]
+    t = O.add(O.add(a, b), ones)
+    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu))
+    _close(y, O.round(t, 1e-8))
+
+
+def test_whole_gpu_direct_svd_branch(ttg):
+    # n = 3, ranks up to 70: at the bond 27 -> 70 the rows (81) lie in [cols, 2 cols)
+    t = O.random([3] * 7, 70, 11, fan_in_scale=True)
+    ranks = O.ranks(t)
+    assert any(c <= r * 3 < 2 * c for r, c in zip(ranks[:-1], ranks[1:]))
+    y = ttg.round(t, _opts(ttg, 1e-10, ttg.schedule.whole_gpu))
+    _close(y, O.round(t, 1e-10))
+
+
+def test_whole_gpu_truncating(ttg):
+    from tensor_train_gb300 import sketch
+    cores, _ = sketch.decaying_tt(5, d=12, n=4, terms=48, rho=0.6, rank8_every=8)
+    t = [np.ascontiguousarray(c) for c in cores]
+    ref = O.round(t, 1e-6)
+    y = ttg.round(t, _opts(ttg, 1e-6, ttg.schedule.whole_gpu))
+    assert max(abs(a - b) for a, b in zip(O.ranks(y), O.ranks(ref))) <= 1
+    assert O.rel_err(y, t) <= 1e-6
+    assert O.rel_err(y, ref) <= 2e-6
+
+
+def test_whole_gpu_matches_per_tt(ttg):
+    a = O.random([8] * 6, 48, 21, fan_in_scale=True)
+    b = O.random([8] * 6, 48, 22, fan_in_scale=True)
+    t = O.add(a, b)
+    y1 = ttg.round(t, _opts(ttg, 1e-9, ttg.schedule.whole_gpu))
+    y2 = ttg.round(t, _opts(ttg, 1e-9, ttg.schedule.per_tt))
+    assert O.ranks(y1) == O.ranks(y2)
+    assert O.rel_err(y1, y2) <= 1e-12
+    _close(y1, O.round(t, 1e-9))
+
+
+def test_whole_gpu_batch_of_two_and_bond_stats(ttg):
+    ts = [O.random_uneven(1000 + i) for i in range(2)]
+    nb = sum(len(t) - 1 for t in ts)
+    stats = np.zeros(4 * nb)
+    stats2 = np.zeros(4 * nb)
+    ys = ttg.round_batch(ts, _opts(ttg, 1e-8, ttg.schedule.whole_gpu, bond_stats=stats))
+    ttg.round_batch(ts, _opts(ttg, 1e-8, ttg.schedule.per_tt, bond_stats=stats2))
+    for y, t in zip(ys, ts):
+        _close(y, O.round(t, 1e-8))
+    s, s2 = stats.reshape(-1, 4), stats2.reshape(-1, 4)
+    assert np.array_equal(s[:, 2:], s2[:, 2:])
+    assert np.allclose(s[:, :2], s2[:, :2], rtol=1e-10, atol=0)
+
+
+def test_whole_gpu_matvec_round_naive(ttg):
+    A = O.random_matrix([4] * 8, [4] * 8, 4, 44, fan_in_scale=True)
+    x = O.random([4] * 8, 24, 45, fan_in_scale=True)
+    # method svd on matvec_round = apply, then round the product
+    y = ttg.matvec_round(A, x, _opts(ttg, 1e-10, ttg.schedule.whole_gpu))
+    _close(y, O.matvec_round(A, x, 1e-10))
+
+
+def test_whole_gpu_mixed_request_is_fp64_exact(ttg):
+    # the whole-GPU sweep computes in FP64 for either precision
+    a = O.random([4] * 8, 40, 31, fan_in_scale=True)
+    b = O.random([4] * 8, 40, 32, fan_in_scale=True)
+    t = O.add(a, b)
+    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu, precision=ttg.precision.mixed))
+    _close(y, O.round(t, 1e-8))
