@@ -401,7 +401,9 @@ int32_t setup_wide(ttg_plan& P)
   const size_t cc = sizeof(double) * static_cast<size_t>(c_max * c_max);
   const size_t cm = sizeof(double) * static_cast<size_t>(core_max);
   const size_t oW = take(cm), oU = take(cm), oP = take(cm), oA = take(cm), oR = take(cc),
-               oV = take(cc), oF = take(cc), otau = take(8 * c_max), osig = take(8 * c_max),
+               oV = take(cc), oF = take(cc), oT1 = take(cc), oT2 = take(cc),
+               opart = take(8 * static_cast<size_t>(grid) + 8), oumax = take(8),
+               otau = take(8 * c_max), osig = take(8 * c_max),
                osorted = take(8 * c_max), oord = take(4 * c_max), ocn = take(8 * (cols_max + 1)),
                oival = take(64), orot = take(4 * ms), orel = take(4 * ms), obar = take(sizeof(GridBar));
   TTG_CUDA(P.wdev.ensure(o));
@@ -426,6 +428,11 @@ int32_t setup_wide(ttg_plan& P)
   j.R = reinterpret_cast<double*>(b + oR);
   j.V = reinterpret_cast<double*>(b + oV);
   j.F = reinterpret_cast<double*>(b + oF);
+  j.T1 = reinterpret_cast<double*>(b + oT1);
+  j.T2 = reinterpret_cast<double*>(b + oT2);
+  j.part = reinterpret_cast<double*>(b + opart);
+  j.umax = reinterpret_cast<unsigned long long*>(b + oumax);
+  j.mixed = P.opts.precision == TTG_PREC_MIXED ? 1 : 0;
   j.tau = reinterpret_cast<double*>(b + otau);
   j.sig = reinterpret_cast<double*>(b + osig);
   j.sorted = reinterpret_cast<double*>(b + osorted);

@@ -130,6 +130,7 @@ struct WideJob
   int max_rank;
   int max_sweeps;
   int jblock;          // Jacobi block width (columns)
+  int mixed;           // 1: FP32 + df64 SVD sweeps
   int64_t smem_doubles;
   double eps;
   double* W;           // core_max: reflectors
@@ -139,12 +140,16 @@ struct WideJob
   double* R;           // c_max^2
   double* V;           // c_max^2
   double* F;           // c_max^2
+  double* T1;          // c_max^2: FP32 V of the mixed SVD
+  double* T2;          // c_max^2: FP64 copy of it
   double* tau;         // c_max
   double* sig;         // c_max
   double* sorted;      // c_max
   int* ord;            // c_max
   double* cn;          // sum of ranks: balancing column norms
   int* ival;           // [0] = truncation rank of the current bond
+  double* part;        // one partial sum per CTA
+  unsigned long long* umax;  // grid-wide max of |x| bit patterns
   unsigned int* sweep_rot;  // max_sweeps
   unsigned int* sweep_rel;  // max_sweeps
   GridBar* bar;

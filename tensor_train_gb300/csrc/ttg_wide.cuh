@@ -18,9 +18,10 @@
 //     ends the round.  Outer sweeps stop when a sweep rotates nothing or its
 //     largest relative rotation is below kJacobiStopRel.
 //   * Contractions: 64x64 FP64 output tiles spread over the CTAs.
-// Arithmetic is FP64 throughout: with one TT on the whole GPU the sweep is
-// bound by the dependency chain (one reflector, one Jacobi round after the
-// other), not by the FP64 pipes.
+// QR, contractions and balancing are FP64.  The SVD is FP64 Jacobi on the
+// plain path; on the mixed path FP32 sweeps do the bulk of the rotating and
+// df64 sweeps (FP32 pipes) polish to FP64-level accuracy, as in the
+// one-CTA-per-TT kernel.
 //
 // Every barrier wait is bounded (kGridWaitCycles): a CTA that gives up sets
 // the shared error word, every other CTA sees it at its next barrier, and
@@ -236,35 +237,39 @@ __device__ void wide_apply_q(const WideJob& job, int h, int kref, const double* 
   }
 }
 
-// One-sided Jacobi of A (p x q, column-major, lda) in block-pair rounds over
-// the grid; V (q x q, ld q) accumulates the rotations when non-null.
-// Returns the outer sweep count; *conv = 0 if max_sweeps was reached.
-__device__ bool wide_jacobi(const WideJob& job, double* A, int p, int q, int64_t lda, double* V,
-                            double floor2, WideSmem sm, CtaShared& sh, int* sweeps_out, int* conv)
+// One-sided Jacobi of A (p x q, column-major, lda; element type E = float,
+// double or df64) in block-pair rounds of b columns over the grid; V (q x q,
+// ld q) accumulates the rotations when non-null.  Stops after a sweep
+// without rotations or whose largest relative rotation is below stop_rel.
+template <class E>
+__device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda, E* V, int b,
+                            typename JOps<E>::S floor2, typename JOps<E>::S stop_rel,
+                            int max_sweeps, WideSmem sm, CtaShared& sh, int* sweeps_out,
+                            int* conv)
 {
+  using S = typename JOps<E>::S;
   const int P = gridDim.x, me = blockIdx.x;
-  const int b = job.jblock;
   const int nblk = (q + b - 1) / b;
   const int NB = nblk + (nblk & 1), npairs = NB / 2;
-  double* As = sm.p;
-  double* Vs = As + static_cast<int64_t>(p) * 2 * b;
-  double* ns = Vs + (V ? static_cast<int64_t>(q) * 2 * b : 0);
+  E* As = reinterpret_cast<E*>(sm.p);
+  E* Vs = As + static_cast<int64_t>(p) * 2 * b;
+  S* ns = reinterpret_cast<S*>(Vs + (V ? static_cast<int64_t>(q) * 2 * b : 0));
   if (me == 0)
-    for (int s = threadIdx.x; s < job.max_sweeps; s += blockDim.x)
+    for (int s = threadIdx.x; s < max_sweeps; s += blockDim.x)
     {
       job.sweep_rot[s] = 0u;
       job.sweep_rel[s] = 0u;
     }
   WSYNC();
   *conv = 0;
-  *sweeps_out = job.max_sweeps;
+  *sweeps_out = max_sweeps;
   if (q < 2)
   {
     *conv = 1;
     *sweeps_out = 0;
     return true;
   }
-  for (int sw = 0; sw < job.max_sweeps; ++sw)
+  for (int sw = 0; sw < max_sweeps; ++sw)
   {
     for (int rr = 0; rr < NB - 1; ++rr)
     {
@@ -293,8 +298,7 @@ __device__ bool wide_jacobi(const WideJob& job, double* A, int p, int q, int64_t
         __syncthreads();
         int lconv = 1;
         float mr = 0.0f;
-        cta_jacobi<double>(As, p, nc, p, V ? Vs : nullptr, q, 1, &lconv, ns, sh, floor2, 0.0, &mr,
-                           q);
+        cta_jacobi<E>(As, p, nc, p, V ? Vs : nullptr, q, 1, &lconv, ns, sh, floor2, S(0), &mr, q);
         if (!lconv && threadIdx.x == 0)
         {
           atomicOr(&job.sweep_rot[sw], 1u);
@@ -317,13 +321,125 @@ __device__ bool wide_jacobi(const WideJob& job, double* A, int p, int q, int64_t
     }
     const unsigned int rot = *reinterpret_cast<volatile unsigned int*>(&job.sweep_rot[sw]);
     const unsigned int rel = *reinterpret_cast<volatile unsigned int*>(&job.sweep_rel[sw]);
-    if (!rot || __uint_as_float(rel) < static_cast<float>(kJacobiStopRel))
+    if (!rot || __uint_as_float(rel) < static_cast<float>(stop_rel))
     {
       *conv = 1;
       *sweeps_out = sw + 1;
       return true;
     }
   }
+  return true;
+}
+
+// Grid-stride loop bounds of this thread.
+#define WIDE_FOR(e, n)                                                                   \
+  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < (n); \
+       e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+
+// The SVD step of the mixed path over the grid, as cta_jacobi_mixed:
+// FP32 block-pair sweeps on an FP32 copy of src (p x q) accumulating V32,
+// two Newton-Schulz steps V <- V (3I - V^T V)/2 in FP64, A = src V
+// (FP64 tiles), then df64 block-pair sweeps on A / 2^e (and on V when
+// with_v) until the rotations fall below kJacobiStopRel.  A (double, p x
+// q, ld p) and, when with_v, V (double, q x q) hold the result.  Returns
+// the df64 sweep count in *sweeps.
+__device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool with_v,
+                               double floor2, WideSmem sm, CtaShared& sh, int* sweeps, int* conv)
+{
+  const int me = blockIdx.x;
+  float* A32 = reinterpret_cast<float*>(job.Pb);
+  float* V32 = reinterpret_cast<float*>(job.T1);
+  const int64_t pq = static_cast<int64_t>(p) * q, qq = static_cast<int64_t>(q) * q;
+  double part = 0.0;
+  WIDE_FOR(e, pq)
+  {
+    const float x = static_cast<float>(src(e % p, e / p));
+    A32[e] = x;
+    part += static_cast<double>(x) * x;
+  }
+  WIDE_FOR(e, qq)
+  V32[e] = (e % q == e / q) ? 1.0f : 0.0f;
+  part = cta_sum(part, sh);
+  if (threadIdx.x == 0)
+    job.part[me] = part;
+  if (me == 0 && threadIdx.x == 0)
+    *job.umax = 0ull;
+  WSYNC();
+  double ss = 0.0;
+  for (int i = 0; i < static_cast<int>(gridDim.x); ++i)
+    ss += job.part[i];
+  const float floor32 = fmaxf(static_cast<float>(floor2), 1e-12f * static_cast<float>(ss / q));
+  int sw32 = 0, cv32 = 0;
+  if (!wide_jacobi<float>(job, A32, p, q, p, V32, 2 * job.jblock, floor32, 3e-4f,
+                          job.max_sweeps < 24 ? job.max_sweeps : 24, sm, sh, &sw32, &cv32))
+    return false;
+  // Two Newton-Schulz steps V <- V (3I - V^T V)/2 in FP64 (M in F): the
+  // FP32 rotations leave V32^T V32 - I at up to ~1e-5 for a few hundred
+  // columns, one step squares that to ~1e-10, the second to FP64 level.
+  double* Vd = job.T2;
+  WIDE_FOR(e, qq)
+  Vd[e] = static_cast<double>(V32[e]);
+  WSYNC();
+  for (int it = 0; it < 2; ++it)
+  {
+    double* Vin = it == 0 ? Vd : job.V;
+    double* Vout = it == 0 ? job.V : Vd;
+    wide_gemm(q, q, q, View{Vin, q, 1}, View{Vin, 1, q}, job.F, 1, q, sh);
+    WSYNC();
+    WIDE_FOR(e, qq)
+    job.F[e] = ((e % q == e / q) ? 1.5 : 0.0) - 0.5 * job.F[e];
+    WSYNC();
+    wide_gemm(q, q, q, View{Vin, 1, q}, View{job.F, 1, q}, Vout, 1, q, sh);
+    WSYNC();
+  }
+  // The result is in Vd (T2); V takes it.
+  wide_copy(job.V, Vd, qq);
+  WSYNC();
+  wide_gemm(p, q, q, src, View{job.V, 1, q}, job.A, 1, p, sh);
+  WSYNC();
+  // df64 polish on A / 2^e, 2^e <= max|A| < 2^(e+1) (bit-pattern max).
+  {
+    unsigned long long mx = 0ull;
+    WIDE_FOR(e, pq)
+    {
+      const unsigned long long bits =
+        static_cast<unsigned long long>(__double_as_longlong(job.A[e])) & 0x7fffffffffffffffull;
+      mx = bits > mx ? bits : mx;
+    }
+    for (int o = 16; o > 0; o >>= 1)
+    {
+      const unsigned long long y = __shfl_xor_sync(0xffffffffu, mx, o);
+      mx = y > mx ? y : mx;
+    }
+    if ((threadIdx.x & 31) == 0)
+      atomicMax(job.umax, mx);
+  }
+  WSYNC();
+  const int ex = static_cast<int>((*reinterpret_cast<volatile unsigned long long*>(job.umax) >> 52) &
+                                  0x7ff);
+  const double sc = (ex == 0 || ex == 0x7ff) ? 1.0 : __longlong_as_double(static_cast<long long>(ex) << 52);
+  const double isc = 1.0 / sc;
+  df64* Ad = reinterpret_cast<df64*>(job.A);
+  df64* Vdd = reinterpret_cast<df64*>(job.V);
+  WIDE_FOR(e, pq)
+  Ad[e] = df_from(job.A[e] * isc);
+  if (with_v)
+  {
+    WIDE_FOR(e, qq)
+    Vdd[e] = df_from(job.V[e]);
+  }
+  WSYNC();
+  if (!wide_jacobi<df64>(job, Ad, p, q, p, with_v ? Vdd : nullptr, job.jblock, floor2 * isc * isc,
+                         kJacobiStopRel, job.max_sweeps, sm, sh, sweeps, conv))
+    return false;
+  WIDE_FOR(e, pq)
+  job.A[e] = df_to(Ad[e]) * sc;
+  if (with_v)
+  {
+    WIDE_FOR(e, qq)
+    job.V[e] = df_to(Vdd[e]);
+  }
+  WSYNC();
   return true;
 }
 
@@ -517,7 +633,13 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
       // A = R (c x c), then Jacobi.
       wide_copy(job.A, job.R, static_cast<int64_t>(c) * c);
       WSYNC();
-      if (!wide_jacobi(job, job.A, c, c, c, nullptr, floor2, sm, sh, &sweeps, &conv))
+      if (job.mixed)
+      {
+        if (!wide_svd_mixed(job, View{job.R, 1, c}, c, c, false, floor2, sm, sh, &sweeps, &conv))
+          return false;
+      }
+      else if (!wide_jacobi<double>(job, job.A, c, c, c, nullptr, job.jblock, floor2,
+                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
         return false;
       if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
         return false;
@@ -542,7 +664,13 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
            e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(gridDim.x) * blockDim.x)
         job.A[e] = X(e % h, e / h);
       WSYNC();
-      if (!wide_jacobi(job, job.A, h, c, h, nullptr, floor2, sm, sh, &sweeps, &conv))
+      if (job.mixed)
+      {
+        if (!wide_svd_mixed(job, X, h, c, false, floor2, sm, sh, &sweeps, &conv))
+          return false;
+      }
+      else if (!wide_jacobi<double>(job, job.A, h, c, h, nullptr, job.jblock, floor2,
+                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
         return false;
       if (!wide_truncate(job, job.A, h, c, h, delta, T, bs, sh))
         return false;
@@ -570,7 +698,13 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
            e < static_cast<int64_t>(h) * h; e += stride)
         job.V[e] = (e % h == e / h) ? 1.0 : 0.0;
       WSYNC();
-      if (!wide_jacobi(job, job.A, c, h, c, job.V, floor2, sm, sh, &sweeps, &conv))
+      if (job.mixed)
+      {
+        if (!wide_svd_mixed(job, transposed(X), c, h, true, floor2, sm, sh, &sweeps, &conv))
+          return false;
+      }
+      else if (!wide_jacobi<double>(job, job.A, c, h, c, job.V, job.jblock, floor2,
+                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
         return false;
       if (!wide_truncate(job, job.A, c, h, c, delta, T, bs, sh))
         return false;
@@ -628,4 +762,5 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
       return;
 }
 
+#undef WIDE_FOR
 #undef WSYNC

@@ -101,10 +101,36 @@ def test_whole_gpu_matvec_round_naive(ttg):
     _close(y, O.matvec_round(A, x, 1e-10))
 
 
-def test_whole_gpu_mixed_request_is_fp64_exact(ttg):
-    # the whole-GPU sweep computes in FP64 for either precision
-    a = O.random([4] * 8, 40, 31, fan_in_scale=True)
-    b = O.random([4] * 8, 40, 32, fan_in_scale=True)
+MIXED_TOL = 1e-10
+
+
+@pytest.mark.parametrize("n,r,seed", [(4, 40, 31), (3, 70, 11), (8, 48, 21)])
+def test_whole_gpu_mixed(ttg, n, r, seed):
+    # FP32 + df64 SVD sweeps over the grid; all three svd_step branches occur
+    a = O.random([n] * 7, r, seed, fan_in_scale=True)
+    b = O.random([n] * 7, r, seed + 1, fan_in_scale=True)
     t = O.add(a, b)
-    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu, precision=ttg.precision.mixed))
-    _close(y, O.round(t, 1e-8))
+    info = ttg.RoundResult()
+    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu, precision=ttg.precision.mixed),
+                  info)
+    _close(y, O.round(t, 1e-8), MIXED_TOL)
+    assert info.converged and info.status == 0
+
+
+def test_whole_gpu_mixed_truncating(ttg):
+    from tensor_train_gb300 import sketch
+    cores, _ = sketch.decaying_tt(9, d=12, n=4, terms=64, rho=0.7, rank8_every=8)
+    t = [np.ascontiguousarray(c) for c in cores]
+    ref = O.round(t, 1e-6)
+    y = ttg.round(t, _opts(ttg, 1e-6, ttg.schedule.whole_gpu, precision=ttg.precision.mixed))
+    assert max(abs(a - b) for a, b in zip(O.ranks(y), O.ranks(ref))) <= 1
+    assert O.rel_err(y, t) <= 1e-6
+    assert O.rel_err(y, ref) <= 2e-6
+
+
+def test_whole_gpu_mixed_matvec_round(ttg):
+    A = O.random_matrix([4] * 8, [4] * 8, 4, 44, fan_in_scale=True)
+    x = O.random([4] * 8, 24, 45, fan_in_scale=True)
+    y = ttg.matvec_round(A, x, _opts(ttg, 1e-10, ttg.schedule.whole_gpu,
+                                     precision=ttg.precision.mixed))
+    _close(y, O.matvec_round(A, x, 1e-10), MIXED_TOL)
