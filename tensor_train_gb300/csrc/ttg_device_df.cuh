@@ -337,7 +337,11 @@ __device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, in
   using S = typename O::S;
   using Acc = typename O::Acc;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int G = m <= 128 ? 8 : (m <= 512 ? 16 : 32);
+  // Group size by column length, widened while half the groups would
+  // already cover all pairs of a round (short rows of few columns).
+  int G = m <= 128 ? 8 : (m <= 512 ? 16 : 32);
+  while (G < 32 && kWarps * (32 / G) >= 2 * ((n + 1) / 2))
+    G *= 2;
   const int gpw = 32 / G, ngroups = kWarps * gpw;
   const int grp = w * gpw + lane / G, gl = lane & (G - 1);
   const int N = n + (n & 1);

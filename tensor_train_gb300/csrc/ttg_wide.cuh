@@ -125,67 +125,82 @@ __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, Ct
       y[i] = X(i, l);
   }
   __syncthreads();
+  // Reflector j from column j (its owner has applied H_0..H_{j-1} to it),
+  // published to W and tau.
+  auto reflect = [&](int j) {
+    const int len = h - j;
+    double* x = col(j) + j;
+    double part = 0.0;
+    for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
+      part += x[i] * x[i];
+    const double tail2 = cta_sum(part, sh);
+    const double x0 = x[0];
+    double beta, t, inv;
+    if (tail2 <= DBL_MIN)
+    {
+      t = 0.0;
+      beta = x0;
+      inv = 0.0;
+    }
+    else
+    {
+      beta = sqrt(x0 * x0 + tail2);
+      if (x0 >= 0.0)
+        beta = -beta;
+      inv = 1.0 / (x0 - beta);
+      t = (beta - x0) / beta;
+    }
+    double* pub = job.W + static_cast<int64_t>(j) * h + j;
+    for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
+    {
+      x[i] *= inv;
+      pub[i] = x[i];
+    }
+    if (threadIdx.x == 0)
+    {
+      x[0] = beta;
+      pub[0] = beta;
+      job.tau[j] = t;
+    }
+  };
+  // y <- H_j y on rows j.. of an owned column.
+  auto apply = [&](int j, double t, const double* v, int l) {
+    const int len = h - j;
+    double* y = col(l) + j;
+    double part = 0.0;
+    for (int i = threadIdx.x; i < len; i += blockDim.x)
+      part += (i == 0 ? 1.0 : v[i]) * y[i];
+    const double dot = cta_sum(part, sh) * t;
+    for (int i = threadIdx.x; i < len; i += blockDim.x)
+      y[i] -= dot * (i == 0 ? 1.0 : v[i]);
+    __syncthreads();
+  };
+  if (k > 0 && me == 0)
+    reflect(0);
   for (int j = 0; j < k; ++j)
   {
-    const int len = h - j;
-    if (j % P == me)
-    {
-      double* x = col(j) + j;
-      double part = 0.0;
-      for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
-        part += x[i] * x[i];
-      const double tail2 = cta_sum(part, sh);
-      const double x0 = x[0];
-      double beta, t, inv;
-      if (tail2 <= DBL_MIN)
-      {
-        t = 0.0;
-        beta = x0;
-        inv = 0.0;
-      }
-      else
-      {
-        beta = sqrt(x0 * x0 + tail2);
-        if (x0 >= 0.0)
-          beta = -beta;
-        inv = 1.0 / (x0 - beta);
-        t = (beta - x0) / beta;
-      }
-      double* pub = job.W + static_cast<int64_t>(j) * h + j;
-      for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
-      {
-        x[i] *= inv;
-        pub[i] = x[i];
-      }
-      if (threadIdx.x == 0)
-      {
-        x[0] = beta;
-        pub[0] = beta;
-        job.tau[j] = t;
-      }
-    }
     if (!grid_sync(job.bar))
     {
       *ok = false;
       return k;
     }
     const double t = job.tau[j];
-    if (t == 0.0)
-      continue;
     const double* v = job.W + static_cast<int64_t>(j) * h + j;
-    for (int l = me; l < c; l += P)
+    // Look-ahead: the owner of column j+1 brings it up to date and forms
+    // reflector j+1 first (the next barrier waits for it), then updates
+    // its other columns.
+    const int nj = j + 1;
+    const bool own_next = nj < k && nj % P == me;
+    if (own_next)
     {
-      if (l <= j)
-        continue;
-      double* y = col(l) + j;
-      double part = 0.0;
-      for (int i = threadIdx.x; i < len; i += blockDim.x)
-        part += (i == 0 ? 1.0 : v[i]) * y[i];
-      const double dot = cta_sum(part, sh) * t;
-      for (int i = threadIdx.x; i < len; i += blockDim.x)
-        y[i] -= dot * (i == 0 ? 1.0 : v[i]);
-      __syncthreads();
+      if (t != 0.0)
+        apply(j, t, v, nj);
+      reflect(nj);
     }
+    if (t != 0.0)
+      for (int l = me; l < c; l += P)
+        if (l > j && !(own_next && l == nj))
+          apply(j, t, v, l);
   }
   // R columns from their owners.
   for (int l = me; l < c; l += P)
@@ -284,17 +299,22 @@ __device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda,
         if (nc < 2)
           continue;
         auto gcol = [&](int j) { return j < np ? c0 + j : c1 + (j - np); };
-        for (int64_t e = threadIdx.x; e < static_cast<int64_t>(p) * nc; e += blockDim.x)
+        // Warp per column, lanes down the rows (no integer division).
+        const int lane = threadIdx.x & 31, wp = threadIdx.x >> 5;
+        for (int j = wp; j < nc; j += kWarps)
         {
-          const int i = static_cast<int>(e % p), j = static_cast<int>(e / p);
-          As[e] = A[i + static_cast<int64_t>(gcol(j)) * lda];
-        }
-        if (V)
-          for (int64_t e = threadIdx.x; e < static_cast<int64_t>(q) * nc; e += blockDim.x)
+          const E* src = A + static_cast<int64_t>(gcol(j)) * lda;
+          E* dst = As + static_cast<int64_t>(j) * p;
+          for (int i = lane; i < p; i += 32)
+            dst[i] = src[i];
+          if (V)
           {
-            const int i = static_cast<int>(e % q), j = static_cast<int>(e / q);
-            Vs[e] = V[i + static_cast<int64_t>(gcol(j)) * q];
+            const E* vs = V + static_cast<int64_t>(gcol(j)) * q;
+            E* vd = Vs + static_cast<int64_t>(j) * q;
+            for (int i = lane; i < q; i += 32)
+              vd[i] = vs[i];
           }
+        }
         __syncthreads();
         int lconv = 1;
         float mr = 0.0f;
@@ -304,17 +324,20 @@ __device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda,
           atomicOr(&job.sweep_rot[sw], 1u);
           atomicMax(&job.sweep_rel[sw], __float_as_uint(mr));
         }
-        for (int64_t e = threadIdx.x; e < static_cast<int64_t>(p) * nc; e += blockDim.x)
+        for (int j = wp; j < nc; j += kWarps)
         {
-          const int i = static_cast<int>(e % p), j = static_cast<int>(e / p);
-          A[i + static_cast<int64_t>(gcol(j)) * lda] = As[e];
-        }
-        if (V)
-          for (int64_t e = threadIdx.x; e < static_cast<int64_t>(q) * nc; e += blockDim.x)
+          E* dst = A + static_cast<int64_t>(gcol(j)) * lda;
+          const E* src = As + static_cast<int64_t>(j) * p;
+          for (int i = lane; i < p; i += 32)
+            dst[i] = src[i];
+          if (V)
           {
-            const int i = static_cast<int>(e % q), j = static_cast<int>(e / q);
-            V[i + static_cast<int64_t>(gcol(j)) * q] = Vs[e];
+            E* vd = V + static_cast<int64_t>(gcol(j)) * q;
+            const E* vs = Vs + static_cast<int64_t>(j) * q;
+            for (int i = lane; i < q; i += 32)
+              vd[i] = vs[i];
           }
+        }
         __syncthreads();
       }
       WSYNC();
