@@ -51,6 +51,11 @@ def parse():
                          "tensor configurations, measured one JSON line each")
     ap.add_argument("--precision", choices=["fp64", "mixed"], default="mixed")
     ap.add_argument("--method", choices=["svd", "svd_streaming"], default="svd")
+    ap.add_argument("--schedule", choices=["auto", "per_tt", "whole_gpu"], default="auto")
+    ap.add_argument("--d", type=int, default=0,
+                    help="number of cores of round_d40 / matvec_d20 (0 = the configuration's; "
+                         "smaller values make short cases for profiling)")
+    ap.add_argument("--samples", type=int, default=1 << 20, help="eval_d32 multi-indices")
     return ap.parse_args()
 
 
@@ -331,41 +336,46 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
-def single_inputs(T, workload):
+def single_inputs(T, workload, d=0, samples=1 << 20):
     """Seeded inputs of the single-tensor configurations (cores scaled by
-    1/sqrt(r_k n_k), or 1/sqrt(r m n) for MPO cores)."""
+    1/sqrt(r_k n_k), or 1/sqrt(r m n) for MPO cores).  d > 0 shortens the
+    train of round_d40 / matvec_d20 (profiling cases)."""
     if workload == "round_d10":
         a = T.random([4] * 10, 8, 42, fan_in_scale=True)
         b = T.random([4] * 10, 8, 43, fan_in_scale=True)
         return {"tt": T.add(a, b), "eps": 1e-8,
                 "desc": "round(add(a,b)): d=10, n=4, a,b random rank 8 (seeds 42/43), eps=1e-8"}
     if workload == "round_d40":
-        a = T.random([8] * 40, 128, 46, fan_in_scale=True)
-        b = T.random([8] * 40, 128, 47, fan_in_scale=True)
+        d = d or 40
+        a = T.random([8] * d, 128, 46, fan_in_scale=True)
+        b = T.random([8] * d, 128, 47, fan_in_scale=True)
         # ones() gets the same 1/sqrt(r n) core scaling as the random terms;
         # unscaled, its norm 8^20 would swamp a + b and the sum rounds to rank 1.
-        ones = [c / (8.0 ** 0.5) for c in T.ones([8] * 40)]
+        ones = [c / (8.0 ** 0.5) for c in T.ones([8] * d)]
         return {"tt": T.add(T.add(a, b), ones), "eps": 1e-8,
-                "desc": "round(a+b+ones): d=40, n=8, a,b random rank 128 (seeds 46/47), "
+                "desc": f"round(a+b+ones): d={d}, n=8, a,b random rank 128 (seeds 46/47), "
                         "ones scaled 1/sqrt(8) per core, interior rank 257, eps=1e-8"}
     if workload == "matvec_d20":
-        A = T.random_matrix([4] * 20, [4] * 20, 8, 44, fan_in_scale=True)
-        x = T.random([4] * 20, 32, 45, fan_in_scale=True)
+        d = d or 20
+        A = T.random_matrix([4] * d, [4] * d, 8, 44, fan_in_scale=True)
+        x = T.random([4] * d, 32, 45, fan_in_scale=True)
         return {"A": A, "x": x, "eps": 1e-10,
-                "desc": "matvec_round(A, x): d=20, m=n=4, MPO rank 8 (seed 44), TT rank 32 "
+                "desc": f"matvec_round(A, x): d={d}, m=n=4, MPO rank 8 (seed 44), TT rank 32 "
                         "(seed 45), eps=1e-10"}
     if workload == "eval_d32":
         import numpy as np
         t = T.random([4] * 32, 64, 48, fan_in_scale=True)
-        idx = np.random.default_rng(49).integers(0, 4, size=(1 << 20, 32)).astype(np.int32)
+        idx = np.random.default_rng(49).integers(0, 4, size=(samples, 32)).astype(np.int32)
         return {"tt": t, "idx": idx,
-                "desc": "eval_batch: d=32, n=4, rank 64 (seed 48), M=2^20 uniform indices "
+                "desc": f"eval_batch: d=32, n=4, rank 64 (seed 48), M={samples} uniform indices "
                         "(numpy seed 49)"}
     raise ValueError(workload)
 
 
 def run_single(args):
-    """One JSON line for a single-tensor configuration (not the headline)."""
+    """One JSON line for a single-tensor configuration (not the headline):
+    the requested precision is the line's value; round / matvec_round lines
+    also time the other precision (mixed vs plain FP64) on the same input."""
     import numpy as np
     import torch
 
@@ -375,96 +385,123 @@ def run_single(args):
     torch.cuda.set_device(0)
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
-    inp = single_inputs(T, args.workload)
-    prec = T.precision[args.precision]
-    line = {"workload": args.workload, "config": {"workload": inp["desc"]},
+    inp = single_inputs(T, args.workload, args.d, args.samples)
+    line = {"workload": args.workload, "metric": METRIC, "config": {"workload": inp["desc"]},
             "steps": args.steps, "warmup": args.warmup, "precision": args.precision}
+
+    def timed(plan):
+        plan.upload(sptr)
+        for _ in range(args.warmup):
+            plan.run(sptr)
+        torch.cuda.synchronize()
+        ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        with Clocks(0) as clk:
+            ev0.record(stream)
+            for _ in range(args.steps):
+                plan.run(sptr)
+            ev1.record(stream)
+            torch.cuda.synchronize()
+        return ev0.elapsed_time(ev1) / args.steps, clk.summary()
+
     if args.workload == "eval_d32":
         idx_pinned = torch.from_numpy(inp["idx"]).pin_memory()
         plan = T.Plan("eval", inp["tt"], idx_pinned)
-        unit = "evaluations/s"
-    elif args.workload == "matvec_d20":
-        opts = T.RoundOptions(eps=inp["eps"], precision=prec,
-                              method=T.round_method[args.method])
-        plan = T.Plan("matvec_round", inp["A"], inp["x"], opts=opts)
-        unit = "matvec_rounds/s"
-        line["method"] = args.method
-    else:
-        opts = T.RoundOptions(eps=inp["eps"], precision=prec)
-        plan = T.Plan("round", [inp["tt"]], opts=opts)
-        unit = "roundings/s"
-    plan.upload(sptr)
-    for _ in range(args.warmup):
-        plan.run(sptr)
-    torch.cuda.synchronize()
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    with Clocks(0) as clk:
-        ev0.record(stream)
-        for _ in range(args.steps):
-            plan.run(sptr)
-        ev1.record(stream)
-        torch.cuda.synchronize()
-    ms = ev0.elapsed_time(ev1) / args.steps
-    if args.workload == "eval_d32":
+        ms, clocks = timed(plan)
         M = inp["idx"].shape[0]
         out = plan.download(sptr)
         ranks = [inp["tt"][0].shape[0]] + [c.shape[-1] for c in inp["tt"]]
         F = eval_flops(ranks, M)
         nbytes = 4 * inp["idx"].size + 8 * M + 8 * sum(c.size for c in inp["tt"])
-        line.update({"value": M / (ms / 1e3), "unit": unit, "ms_per_step": ms,
+        peak = max(T.device_fp64_peak() for _ in range(3))
+        line.update({"value": M / (ms / 1e3), "unit": "evaluations/s", "ms_per_step": ms,
+                     "dtype": "f64", "clocks": clocks,
                      "roofline": {"bound": "fp64", "achieved": F / (ms / 1e3) / 1e12,
-                                  "peak": max(T.device_fp64_peak() for _ in range(3)),
-                                  "unit": "TFLOP/s", "hbm_gbs": nbytes / (ms / 1e3) / 1e9,
+                                  "peak": peak, "unit": "TFLOP/s", "frac": F / (ms / 1e3) / 1e12 / peak,
+                                  "hbm_gbs": nbytes / (ms / 1e3) / 1e9,
                                   "bytes_per_launch": nbytes, "flops_per_launch": F}})
-        line["roofline"]["frac"] = line["roofline"]["achieved"] / line["roofline"]["peak"]
-        from oracle import pyoracle as O
-        sel = np.arange(0, M, M // 4096)
-        t0 = time.perf_counter()
-        ref = O.eval_batch(inp["tt"], inp["idx"][sel])
-        sec = time.perf_counter() - t0
-        line["cpu_baseline"] = {"value": len(sel) / sec, "unit": unit, "cores": 1,
-                                "kind": "port", "sample": f"{len(sel)} of the {M} indices"}
-        line["parity_max_abs_err"] = float(np.max(np.abs(out[sel] - ref)))
+        if not args.no_cpu_baseline:
+            from oracle import pyoracle as O
+            sel = np.arange(0, M, max(1, M // 4096))
+            t0 = time.perf_counter()
+            ref = O.eval_batch(inp["tt"], inp["idx"][sel])
+            sec = time.perf_counter() - t0
+            line["cpu_baseline"] = {"value": len(sel) / sec, "unit": "evaluations/s", "cores": 1,
+                                    "kind": "port", "sample": f"{len(sel)} of the {M} indices"}
+            line["parity_max_abs_err"] = float(np.max(np.abs(out[sel] - ref)))
+        print(json.dumps(line), flush=True)
+        return
+
+    matvec = args.workload == "matvec_d20"
+    unit = "matvec_rounds/s" if matvec else "roundings/s"
+    if matvec:
+        A, x = inp["A"], inp["x"]
+        ra = [A[0].shape[0]] + [c.shape[-1] for c in A]
+        rx = [x[0].shape[0]] + [c.shape[-1] for c in x]
+        rin = [a * b for a, b in zip(ra, rx)]
+        modes = [c.shape[1] for c in A]
+        line["method"] = args.method
     else:
+        t = inp["tt"]
+        modes = [c.shape[1] for c in t]
+        rin = [t[0].shape[0]] + [c.shape[-1] for c in t]
+    peak = max(T.device_fp64_peak() for _ in range(3))
+
+    def measure(prec):
+        opts = T.RoundOptions(eps=inp["eps"], precision=T.precision[prec],
+                              schedule=T.schedule[args.schedule],
+                              method=T.round_method[args.method] if matvec else T.round_method.svd)
+        plan = (T.Plan("matvec_round", inp["A"], inp["x"], opts=opts) if matvec
+                else T.Plan("round", [inp["tt"]], opts=opts))
+        ms, clocks = timed(plan)
         kms = []
         for _ in range(3):
             plan.run(sptr)
             kms.append(plan.kernel_ms())
-        outs = plan.download(sptr)
-        y = outs[0]
+        y = plan.download(sptr)[0]
+        sched = plan.schedule()
+        plan.close()
         rout = [y[0].shape[0]] + [c.shape[-1] for c in y]
-        if args.workload == "matvec_d20":
-            A, x = inp["A"], inp["x"]
-            ra = [A[0].shape[0]] + [c.shape[-1] for c in A]
-            rx = [x[0].shape[0]] + [c.shape[-1] for c in x]
-            rin = [a * b for a, b in zip(ra, rx)]
-            modes = [c.shape[1] for c in A]
-            F = matvec_flops(ra, rx, modes, [c.shape[2] for c in A]) + \
-                round_flops(modes, rin, rout)
-        else:
-            t = inp["tt"]
-            modes = [c.shape[1] for c in t]
-            F = round_flops(modes, [t[0].shape[0]] + [c.shape[-1] for c in t], rout)
-        peak = max(T.device_fp64_peak() for _ in range(3))
+        F = round_flops(modes, rin, rout)
+        if matvec:
+            F += matvec_flops(ra, rx, modes, [c.shape[2] for c in A])
         kernel_ms = statistics.mean(kms)
-        line.update({"value": 1e3 / ms, "unit": unit, "ms_per_step": ms, "ranks_out": rout,
-                     "roofline": {"bound": "fp64", "achieved": F / (kernel_ms / 1e3) / 1e12,
-                                  "peak": peak, "unit": "TFLOP/s", "kernel_ms": kernel_ms,
-                                  "flops_per_launch": F}})
-        line["roofline"]["frac"] = line["roofline"]["achieved"] / peak
-        if not args.no_cpu_baseline:
-            from oracle import pyoracle as O
-            t0 = time.perf_counter()
-            if args.workload == "matvec_d20":
-                ref = O.matvec_round(inp["A"], inp["x"], inp["eps"], method=args.method)
-            else:
-                ref = O.round(inp["tt"], inp["eps"])
-            sec = time.perf_counter() - t0
-            line["cpu_baseline"] = {"value": 1.0 / sec, "unit": unit, "cores": 1,
-                                    "kind": "port", "sample": "one full call (oracle, 1 thread)"}
-            line["parity"] = {"ranks_equal": O.ranks(ref) == rout,
-                              "rel_err_vs_oracle": O.rel_err(y, ref)}
-    line["clocks"] = clk.summary()
+        return {"y": y, "ranks_out": rout, "ms": ms, "kernel_ms": kernel_ms, "clocks": clocks,
+                "schedule": sched, "flops": F,
+                "achieved": F / (kernel_ms / 1e3) / 1e12}
+
+    main = measure(args.precision)
+    other_prec = "fp64" if args.precision == "mixed" else "mixed"
+    other = measure(other_prec)
+    mixed, plain = (main, other) if args.precision == "mixed" else (other, main)
+    line.update({"value": 1e3 / main["ms"], "unit": unit, "ms_per_step": main["ms"],
+                 "dtype": "f64" if args.precision == "fp64" else "f64 (fp32/df64 sweeps)",
+                 "schedule": main["schedule"], "ranks_out": main["ranks_out"],
+                 "clocks": main["clocks"],
+                 "roofline": {"bound": "fp64", "achieved": main["achieved"], "peak": peak,
+                              "unit": "TFLOP/s", "frac": main["achieved"] / peak,
+                              "kernel_ms": main["kernel_ms"], "flops_per_launch": main["flops"],
+                              "flop_model": "algorithmic F_round (+ F_matvec) "
+                                            "(tensor_train_gb300/flops.py)"},
+                 other_prec if other_prec == "mixed" else "plain_fp64":
+                     {"value": 1e3 / other["ms"], "ms_per_step": other["ms"],
+                      "kernel_ms": other["kernel_ms"], "schedule": other["schedule"]},
+                 "speedup_mixed_vs_plain_fp64": plain["ms"] / mixed["ms"]})
+    if not args.no_cpu_baseline:
+        from oracle import pyoracle as O
+        t0 = time.perf_counter()
+        if matvec:
+            ref = O.matvec_round(inp["A"], inp["x"], inp["eps"], method=args.method)
+        else:
+            ref = O.round(inp["tt"], inp["eps"])
+        sec = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": 1.0 / sec, "unit": unit, "cores": 1, "kind": "port",
+                                "sample": "one full call (oracle, 1 thread; a single TT does "
+                                          "not split over threads)"}
+        line["parity"] = {
+            "ranks_equal_mixed": O.ranks(ref) == mixed["ranks_out"],
+            "ranks_equal_fp64": O.ranks(ref) == plain["ranks_out"],
+            "rel_err_mixed_vs_oracle": O.rel_err(mixed["y"], ref),
+            "rel_err_fp64_vs_oracle": O.rel_err(plain["y"], ref)}
     print(json.dumps(line), flush=True)
 
 

@@ -247,6 +247,9 @@ int32_t ttg_plan_download(ttg_plan* plan, void* stream, ttg_tensor* outs, double
 /* Device time (ms) of the sweep kernel of the last run(), from events
  * recorded on the run's stream around that launch alone. */
 int32_t ttg_plan_kernel_ms(ttg_plan* plan, float* ms);
+/* Schedule the plan's sweep runs on: TTG_SCHED_PER_TT or
+ * TTG_SCHED_WHOLE_GPU (0 for plans without a rounding sweep). */
+int32_t ttg_plan_schedule(const ttg_plan* plan);
 /* Bytes moved host->device by upload and device->host by download. */
 int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);
 void ttg_plan_destroy(ttg_plan* plan);

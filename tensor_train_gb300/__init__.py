@@ -172,6 +172,7 @@ def lib():
         "ttg_host_axpby": (C.c_int32, [C.c_double, T, C.c_double, T, T]),
         "ttg_host_last_error": (C.c_char_p, []),
         "ttg_device_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
+        "ttg_plan_schedule": (C.c_int32, [C.c_void_p]),
         "ttg_tc_gemm_f32": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                         C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
                                         C.c_int64, C.c_int32, C.c_void_p]),
@@ -442,6 +443,11 @@ class Plan:
         v = C.c_float()
         _check(lib().ttg_plan_kernel_ms(self.h, C.byref(v)), "plan_kernel_ms")
         return v.value
+
+    def schedule(self) -> str:
+        """'per_tt' or 'whole_gpu' (the device schedule of the sweep), '' if none."""
+        v = lib().ttg_plan_schedule(self.h)
+        return {1: "per_tt", 2: "whole_gpu"}.get(v, "")
 
     def io_bytes(self):
         a, b = C.c_int64(), C.c_int64()

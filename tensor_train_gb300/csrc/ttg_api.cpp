@@ -973,6 +973,13 @@ int32_t ttg_plan_kernel_ms(ttg_plan* P, float* ms)
   return TTG_OK;
 }
 
+int32_t ttg_plan_schedule(const ttg_plan* P)
+{
+  if (!P || P->order.empty() || P->job_kind < 0)
+    return 0;
+  return P->wide ? TTG_SCHED_WHOLE_GPU : TTG_SCHED_PER_TT;
+}
+
 int32_t ttg_plan_io_bytes(const ttg_plan* P, int64_t* h2d, int64_t* d2h)
 {
   if (!P)
