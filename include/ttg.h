@@ -64,10 +64,12 @@ typedef enum ttg_method {
 typedef enum ttg_gauge { TTG_GAUGE_NONE = 0, TTG_GAUGE_RIGHT_CANONICAL = 1 } ttg_gauge;
 
 /* Arithmetic of the sweeps.  FP64: every operation in FP64 (the plain
- * rounder).  MIXED: the Jacobi SVD sweeps run in FP32 and one FP64
- * refinement (Newton-Schulz re-orthogonalisation of the FP32 rotations, then
- * FP64 Jacobi polish) restores FP64 accuracy of the singular vectors and
- * values; QR and contractions stay FP64. */
+ * rounder).  MIXED: the Jacobi SVD sweeps run in FP32, a Newton-Schulz
+ * re-orthogonalisation of the FP32 rotations and df64 (two-float) polish
+ * sweeps restore FP64-level accuracy of the singular vectors and values;
+ * on the one-CTA-per-TT schedule the Householder QR and the contractions
+ * run in df64 as well (FP32 pipes), on the whole-GPU schedule they stay
+ * FP64.  Ranks, norms and truncation thresholds are FP64 throughout. */
 typedef enum ttg_precision { TTG_PREC_FP64 = 0, TTG_PREC_MIXED = 1 } ttg_precision;
 
 /* Device schedule of a round (gauge none, method svd): one CTA per TT with
@@ -239,6 +241,18 @@ int32_t ttg_plan_upload(ttg_plan* plan, void* stream);
  * (the deep copy of round(const tt&), round/tt_round.hpp:129-134) and runs
  * the sweep on it.  Idempotent: repeated runs give the same result. */
 int32_t ttg_plan_run(ttg_plan* plan, void* stream);
+/* Autotuner: times the plan's launch configurations on the plan itself
+ * (per-TT schedule: 1 or 2 CTAs per SM, i.e. 200 or 92 KB of shared staging
+ * per CTA; whole-GPU schedule: Jacobi block widths 2/4/8, and the per-TT
+ * schedule as a contender) and keeps the fastest.  *choice (optional): 1 or
+ * 2 = per TT with that many CTAs per SM, 100 + b = whole GPU with block
+ * width b, 0 = nothing to tune.  Synchronises `stream`; drops a captured
+ * graph (capture again afterwards). */
+int32_t ttg_plan_autotune(ttg_plan* plan, void* stream, int32_t* choice);
+/* enable != 0: capture one run (deep copy from the pristine inputs, the
+ * sweep launch, its timing events) as a CUDA graph; later ttg_plan_run calls
+ * replay it with one cudaGraphLaunch.  enable == 0 drops the graph. */
+int32_t ttg_plan_graph(ttg_plan* plan, int32_t enable);
 /* Copies results back (device -> host) and synchronises `stream`.
  * For round plans `outs` receives `count` tensors; for eval plans
  * `values` receives M doubles. */

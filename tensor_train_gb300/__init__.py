@@ -173,6 +173,8 @@ def lib():
         "ttg_host_last_error": (C.c_char_p, []),
         "ttg_device_fp64_peak": (C.c_int32, [C.POINTER(C.c_double)]),
         "ttg_plan_schedule": (C.c_int32, [C.c_void_p]),
+        "ttg_plan_graph": (C.c_int32, [C.c_void_p, C.c_int32]),
+        "ttg_plan_autotune": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
         "ttg_tc_gemm_f32": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                         C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
                                         C.c_int64, C.c_int32, C.c_void_p]),
@@ -422,6 +424,22 @@ class Plan:
 
     def run(self, stream=0):
         _check(lib().ttg_plan_run(self.h, C.c_void_p(stream)), "plan_run")
+
+    def autotune(self, stream=0) -> str:
+        """Time the plan's launch configurations and keep the fastest; returns
+        e.g. 'per_tt x2' or 'whole_gpu b=4' ('' when there is nothing to tune)."""
+        c = C.c_int32()
+        _check(lib().ttg_plan_autotune(self.h, C.c_void_p(stream), C.byref(c)), "plan_autotune")
+        v = c.value
+        if v in (1, 2):
+            return f"per_tt x{v}"
+        if v > 100:
+            return f"whole_gpu b={v - 100}"
+        return ""
+
+    def graph(self, enable: bool = True):
+        """Capture one run as a CUDA graph; run() then replays it."""
+        _check(lib().ttg_plan_graph(self.h, 1 if enable else 0), "plan_graph")
 
     def download(self, stream=0, values=None):
         if self.kind == "eval":

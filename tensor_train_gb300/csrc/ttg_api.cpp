@@ -13,6 +13,7 @@
 #include <mutex>
 #include <numeric>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include <cuda_runtime.h>
@@ -191,6 +192,45 @@ struct HostPinned
 
 size_t align256(size_t b) { return (b + 255) & ~static_cast<size_t>(255); }
 
+// fn(i) for i in [0, n) on up to 16 host threads (packing and unpacking of
+// many tensors is memcpy-bound; one thread would take longer than the
+// sweep).  Returns the first non-OK status.
+template <class Fn>
+int32_t parallel_for(int64_t n, Fn fn)
+{
+  const int64_t hw = std::max<int64_t>(1, std::thread::hardware_concurrency());
+  const int64_t nt = std::min<int64_t>({16, hw, n});
+  if (nt <= 1)
+  {
+    for (int64_t i = 0; i < n; ++i)
+      if (int32_t st = fn(i))
+        return st;
+    return TTG_OK;
+  }
+  std::atomic<int64_t> next{0};
+  std::atomic<int32_t> first{TTG_OK};
+  std::vector<std::string> errs(static_cast<size_t>(nt));
+  std::vector<std::thread> pool;
+  for (int64_t t = 0; t < nt; ++t)
+    pool.emplace_back([&, t] {
+      for (int64_t i = next++; i < n; i = next++)
+        if (int32_t st = fn(i))
+        {
+          int32_t expect = TTG_OK;
+          if (first.compare_exchange_strong(expect, st))
+            errs[static_cast<size_t>(t)] = g_err;
+          return;
+        }
+    });
+  for (auto& th : pool)
+    th.join();
+  if (first.load() != TTG_OK)
+    for (auto& e : errs)
+      if (!e.empty())
+        g_err = e;
+  return first.load();
+}
+
 // --------------------------------------------------------------------------
 // Round plan: arena + tables + scratch in one device allocation; the
 // uploaded prefix [arena | slots | tts | order | idx tables] mirrors a
@@ -252,8 +292,22 @@ struct ttg_plan
   int64_t h2d = 0, d2h = 0;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, evk0 = nullptr, evk1 = nullptr;
   bool kernel_timed = false;
+  // one run captured as a CUDA graph (ttg_plan_graph)
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t gexec = nullptr;
+  int64_t graph_launches = 0;
+  void drop_graph()
+  {
+    if (gexec)
+      cudaGraphExecDestroy(gexec);
+    if (graph)
+      cudaGraphDestroy(graph);
+    gexec = nullptr;
+    graph = nullptr;
+  }
   ~ttg_plan()
   {
+    drop_graph();
     for (cudaEvent_t e : {ev0, ev1, evk0, evk1})
       if (e)
         cudaEventDestroy(e);
@@ -488,18 +542,19 @@ int32_t layout_and_alloc(ttg_plan& P)
   TTG_CUDA(cudaEventCreate(&P.ev1));
   TTG_CUDA(cudaEventCreate(&P.evk0));
   TTG_CUDA(cudaEventCreate(&P.evk1));
-  // Host image of the prefix: arena inputs + tables.
+  // Host image of the prefix: arena inputs + tables.  Only the tables are
+  // cleared; every arena byte a sweep reads is a copied input.
   char* h = static_cast<char*>(P.host.p);
-  std::memset(h, 0, P.prefix_bytes);
+  std::memset(h + P.off_slots, 0, P.prefix_bytes - P.off_slots);
   double* arena = reinterpret_cast<double*>(h + P.off_arena);
-  for (size_t t = 0; t < P.shapes.size(); ++t)
-  {
-    const Shape& s = P.shapes[t];
-    const TTInfo& ti = P.tts[t];
+  parallel_for(static_cast<int64_t>(P.shapes.size()), [&](int64_t t) -> int32_t {
+    const Shape& s = P.shapes[static_cast<size_t>(t)];
+    const TTInfo& ti = P.tts[static_cast<size_t>(t)];
     for (int k = 0; k < s.d; ++k)
       std::memcpy(arena + P.slots[ti.first + k].off, s.data + s.src_off[k],
                   sizeof(double) * static_cast<size_t>(s.size[k]));
-  }
+    return TTG_OK;
+  });
   std::memcpy(h + P.off_slots, P.slots.data(), sizeof(CoreSlot) * P.slots.size());
   std::memcpy(h + P.off_tts, P.tts.data(), sizeof(TTInfo) * P.tts.size());
   std::memcpy(h + P.off_order, P.order.data(), sizeof(int32_t) * P.order.size());
@@ -959,7 +1014,147 @@ int32_t ttg_plan_run(ttg_plan* P, void* stream)
 {
   if (!P)
     return fail(TTG_ERR_ARG, "null plan");
+  if (P->gexec)
+  {
+    TTG_CUDA(cudaGraphLaunch(P->gexec, static_cast<cudaStream_t>(stream)));
+    g_launches += P->graph_launches;
+    return TTG_OK;
+  }
   return plan_run(*P, static_cast<cudaStream_t>(stream));
+}
+
+// Autotuner: times each launch configuration of the plan's sweep on the
+// plan itself (every run restarts from the pristine inputs) and keeps the
+// fastest.  Per-TT schedule: one CTA per SM with 200 KB of shared staging,
+// or two per SM with 92 KB each.  Whole-GPU schedule: Jacobi block widths
+// 2, 4 and 8 columns, and the per-TT schedule as a contender.
+int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  if (choice)
+    *choice = 0;
+  if (P->kind == kPlanEval || P->order.empty() || P->job_kind < 0)
+    return TTG_OK;
+  P->drop_graph();
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  const int sms = std::max(device().sms, 1);
+  const int items = static_cast<int>(P->order.size());
+  struct Cand
+  {
+    int code;  // 1/2: per TT, CTAs per SM; 100 + b: whole GPU with block width b
+    bool wide;
+    int grid, smem, jblock;
+  };
+  std::vector<Cand> cands;
+  const int g1 = std::max(1, std::min(items, sms)), g2 = std::max(1, std::min(items, 2 * sms));
+  cands.push_back({1, false, g1, kSmemOnePerSm, P->wjob.jblock});
+  if (g2 > g1)
+    cands.push_back({2, false, g2, kSmemTwoPerSm, P->wjob.jblock});
+  const bool can_wide = P->wide_grid > 0 && P->wjob.W != nullptr;
+  if (can_wide)
+  {
+    int64_t c_max = 1;
+    for (int t : P->order)
+      for (int k = 0; k < P->tts[t].d; ++k)
+      {
+        const CoreSlot& c = P->slots[P->tts[t].first + k];
+        c_max = std::max<int64_t>(c_max, std::max(c.r, c.rp));
+      }
+    for (int b : {2, 4, 8})
+      if ((6 * c_max + 2) * b <= kSmemOnePerSm)
+        cands.push_back({100 + b, true, P->wide_grid, kSmemOnePerSm, b});
+  }
+  const bool wide0 = P->wide;
+  const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock;
+  float best = 0.0f;
+  int bi = -1;
+  for (size_t i = 0; i < cands.size(); ++i)
+  {
+    const Cand& c = cands[i];
+    P->wide = c.wide;
+    P->grid = c.grid;
+    P->smem_doubles = c.smem;
+    P->wjob.jblock = c.jblock;
+    float ms = 0.0f;
+    for (int rep = 0; rep < 2; ++rep)  // warm, then timed
+    {
+      TTG_CUDA(cudaEventRecord(P->ev0, st));
+      if (int32_t e = plan_run(*P, st))
+        return e;
+      TTG_CUDA(cudaEventRecord(P->ev1, st));
+      TTG_CUDA(cudaEventSynchronize(P->ev1));
+      TTG_CUDA(cudaEventElapsedTime(&ms, P->ev0, P->ev1));
+    }
+    if (P->wide)
+    {
+      GridBar bar{};
+      TTG_CUDA(cudaMemcpy(&bar, P->wjob.bar, sizeof(GridBar), cudaMemcpyDeviceToHost));
+      if (bar.err)
+        return fail(TTG_ERR_TIMEOUT, "autotune: a grid barrier wait timed out");
+    }
+    if (bi < 0 || ms < best)
+    {
+      best = ms;
+      bi = static_cast<int>(i);
+    }
+  }
+  if (bi < 0)
+  {
+    P->wide = wide0;
+    P->grid = grid0;
+    P->smem_doubles = smem0;
+    P->wjob.jblock = jb0;
+    return TTG_OK;
+  }
+  const Cand& c = cands[static_cast<size_t>(bi)];
+  P->wide = c.wide;
+  P->grid = c.grid;
+  P->smem_doubles = c.smem;
+  P->wjob.jblock = c.jblock;
+  if (choice)
+    *choice = c.code;
+  return TTG_OK;
+}
+
+int32_t ttg_plan_graph(ttg_plan* P, int32_t enable)
+{
+  if (!P)
+    return fail(TTG_ERR_ARG, "null plan");
+  P->drop_graph();
+  if (!enable)
+    return TTG_OK;
+  // Capture on a private stream: the legacy default stream cannot capture,
+  // and the instantiated graph launches on any stream.
+  cudaStream_t cap = nullptr;
+  TTG_CUDA(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+  const int64_t l0 = g_launches.load();
+  cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+  int32_t st = TTG_OK;
+  if (e == cudaSuccess)
+  {
+    st = plan_run(*P, cap);
+    const cudaError_t e2 = cudaStreamEndCapture(cap, &P->graph);
+    if (st == TTG_OK && e2 != cudaSuccess)
+      e = e2;
+  }
+  P->graph_launches = g_launches.load() - l0;
+  g_launches -= P->graph_launches;  // capture launches nothing
+  if (e == cudaSuccess && st == TTG_OK)
+    e = cudaGraphInstantiate(&P->gexec, P->graph, 0);
+  cudaStreamDestroy(cap);
+  if (st != TTG_OK)
+  {
+    P->drop_graph();
+    return st;
+  }
+  if (e != cudaSuccess)
+  {
+    P->drop_graph();
+    cudaGetLastError();
+    return fail(TTG_ERR_CUDA, std::string("plan graph capture: ") + cudaGetErrorString(e));
+  }
+  return TTG_OK;
 }
 
 int32_t ttg_plan_kernel_ms(ttg_plan* P, float* ms)
@@ -1061,24 +1256,28 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
     return st;
   const char* h = static_cast<const char*>(P.host.p);
   const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
-  for (int i = 0; i < count; ++i)
-  {
+  const int32_t est = parallel_for(count, [&](int64_t ii) -> int32_t {
+    const int i = static_cast<int>(ii);
     const Shape& s = P.shapes[i];
     if (s.d <= 1)
     {
-      copy_through(s, &outs[i]);
+      if (int32_t e = copy_through(s, &outs[i]))
+        return e;
       if (results)
       {
         std::memset(&results[i], 0, sizeof(results[i]));
         results[i].iters_run = 1;
         results[i].converged = 1;
       }
-      continue;
+      return TTG_OK;
     }
     if (int32_t e = emit_tensor(P, i, s.matrix, s.m, s.n, &outs[i]))
       return e;
     fill_result(T[i], ms, results ? &results[i] : nullptr);
-  }
+    return TTG_OK;
+  });
+  if (est)
+    return est;
   if (int32_t bad = first_bad_status(P))
     return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
   return TTG_OK;

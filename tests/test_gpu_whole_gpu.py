@@ -134,3 +134,24 @@ def test_whole_gpu_mixed_matvec_round(ttg):
     y = ttg.matvec_round(A, x, _opts(ttg, 1e-10, ttg.schedule.whole_gpu,
                                      precision=ttg.precision.mixed))
     _close(y, O.matvec_round(A, x, 1e-10), MIXED_TOL)
+
+
+@pytest.mark.parametrize("sched", ["per_tt", "whole_gpu"])
+def test_plan_graph_replay_matches_direct_runs(ttg, sched):
+    # one run captured as a CUDA graph replays to the same result
+    ts = [O.random_uneven(2000 + i) for i in range(3)]
+    o = _opts(ttg, 1e-8, ttg.schedule[sched], precision=ttg.precision.mixed)
+    plan = ttg.Plan("round", ts, opts=o)
+    plan.upload()
+    plan.run()
+    direct = plan.download()
+    plan.graph(True)
+    for _ in range(2):
+        plan.run()
+    replay = plan.download()
+    assert plan.kernel_ms() > 0.0
+    plan.close()
+    for a, b, t in zip(direct, replay, ts):
+        assert O.ranks(a) == O.ranks(b)
+        assert O.rel_err(a, b) == 0.0
+        _close(a, O.round(t, 1e-8), MIXED_TOL)
