@@ -702,6 +702,16 @@ int32_t plan_upload(ttg_plan& P, cudaStream_t st)
   return TTG_OK;
 }
 
+// Event record that also works inside a stream capture: there it becomes
+// an event-record node of the graph, so every replay records the event.
+cudaError_t record_event(cudaEvent_t ev, cudaStream_t st)
+{
+  cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cs) == cudaSuccess && cs == cudaStreamCaptureStatusActive)
+    return cudaEventRecordWithFlags(ev, st, cudaEventRecordExternal);
+  return cudaEventRecord(ev, st);
+}
+
 int32_t plan_run(ttg_plan& P, cudaStream_t st)
 {
   char* d = static_cast<char*>(P.dev.p);
@@ -734,7 +744,7 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
     TTG_CUDA(cudaMemsetAsync(d + P.off_queue, 0, sizeof(int32_t), st));
     if (P.opts.bond_stats)
       TTG_CUDA(cudaMemsetAsync(d + P.off_stats, 0, sizeof(BondStat) * P.slots.size(), st));
-    TTG_CUDA(cudaEventRecord(P.evk0, st));
+    TTG_CUDA(record_event(P.evk0, st));
     if (P.wide)
     {
       TTG_CUDA(cudaMemsetAsync(P.wjob.bar, 0, sizeof(GridBar), st));
@@ -742,7 +752,7 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
     }
     else
       launch_round(make_job(P), P.grid, st);
-    TTG_CUDA(cudaEventRecord(P.evk1, st));
+    TTG_CUDA(record_event(P.evk1, st));
     P.kernel_timed = true;
     g_launches += 1;
   }

@@ -12,6 +12,10 @@
 
 namespace ttg
 {
+// Internal linkage: every translation unit that includes this header gets
+// its own copy of these device functions.
+namespace
+{
 
 constexpr int kThreads = 256;
 constexpr int kWarps = kThreads / 32;
@@ -119,7 +123,7 @@ __device__ void cta_copy_to_rowmajor(double* dst, int64_t ld, View src, int64_t 
 // convention of Eigen's makeHouseholder (beta = -sign(x0)*||x||; an exactly
 // zero tail gives tau = 0), as in qr_thin (types/tt_eigen_bridge.hpp:42-60).
 // ---------------------------------------------------------------------------
-__device__ void cta_householder_qr(double* A, int m, int c, int64_t ld, double* tau, CtaShared& sh)
+__device__ __noinline__ void cta_householder_qr(double* A, int m, int c, int64_t ld, double* tau, CtaShared& sh)
 {
   const int k = m < c ? m : c;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -187,7 +191,7 @@ __device__ void cta_extract_r(double* R, const double* A, int k, int c, int64_t 
 
 // Form the thin Q (m x k) in place from the reflectors (LAPACK dorg2r order).
 // R must have been extracted before.
-__device__ void cta_form_q(double* A, int m, int k, int64_t ld, const double* tau)
+__device__ __noinline__ void cta_form_q(double* A, int m, int k, int64_t ld, const double* tau)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = k - 1; j >= 0; --j)
@@ -220,7 +224,7 @@ __device__ void cta_form_q(double* A, int m, int k, int64_t ld, const double* ta
 }
 
 // B (m x p, column-major, ldb) <- H_0 H_1 ... H_{kref-1} B.
-__device__ void cta_apply_q(const double* A, int m, int kref, int64_t lda, const double* tau,
+__device__ __noinline__ void cta_apply_q(const double* A, int m, int kref, int64_t lda, const double* tau,
                             double* B, int p, int64_t ldb)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -361,7 +365,7 @@ __device__ void cta_gemm_tile(int i0, int j0, int M, int N, int K, View A, View 
     }
 }
 
-__device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
+__device__ __noinline__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
                          int64_t c_cs, CtaShared& sh)
 {
   for (int i0 = 0; i0 < M; i0 += 64)
@@ -370,4 +374,5 @@ __device__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t
   __syncthreads();
 }
 
+}  // namespace
 }  // namespace ttg

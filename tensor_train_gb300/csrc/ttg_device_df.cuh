@@ -11,6 +11,10 @@
 
 namespace ttg
 {
+// Internal linkage: every translation unit that includes this header gets
+// its own copy of these device functions.
+namespace
+{
 
 // Sum over the CTA in df64; every thread gets the same value.
 __device__ df64 cta_sum_df(df64 v, CtaShared& sh)
@@ -78,7 +82,7 @@ __device__ void cta_split_to_df(df64* W, int64_t ld, View X, int64_t m, int64_t 
 
 // Householder QR in df64, in place (see cta_householder_qr for the layout
 // and convention).  tau is kept in df64.
-__device__ void cta_householder_qr_df(df64* A, int m, int c, int64_t ld, df64* tau, CtaShared& sh)
+__device__ __noinline__ void cta_householder_qr_df(df64* A, int m, int c, int64_t ld, df64* tau, CtaShared& sh)
 {
   const int k = m < c ? m : c;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -150,7 +154,7 @@ __device__ void cta_extract_r_df(double* R, const df64* A, int k, int c, int64_t
 }
 
 // Thin Q (m x k) in place, df64 (dorg2r order, as cta_form_q).
-__device__ void cta_form_q_df(df64* A, int m, int k, int64_t ld, const df64* tau)
+__device__ __noinline__ void cta_form_q_df(df64* A, int m, int k, int64_t ld, const df64* tau)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j = k - 1; j >= 0; --j)
@@ -187,7 +191,7 @@ __device__ void cta_form_q_df(df64* A, int m, int k, int64_t ld, const df64* tau
 }
 
 // B (m x p, column-major df64, ldb) <- H_0 ... H_{kref-1} B.
-__device__ void cta_apply_q_df(const df64* A, int m, int kref, int64_t lda, const df64* tau,
+__device__ __noinline__ void cta_apply_q_df(const df64* A, int m, int kref, int64_t lda, const df64* tau,
                                df64* B, int p, int64_t ldb)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -328,7 +332,7 @@ struct JOps<df64>
 // is below stop_rel ends the iteration (one-sided Jacobi converges
 // quadratically, so the next sweep's rotations would be ~stop_rel^2).
 template <class E>
-__device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, int max_sweeps,
+__device__ __noinline__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, int max_sweeps,
                           int* converged, typename JOps<E>::S* nrm, CtaShared& sh,
                           typename JOps<E>::S floor2 = 0, typename JOps<E>::S stop_rel = 0,
                           float* maxrel_out = nullptr, int vrows = -1)
@@ -481,7 +485,7 @@ __device__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, int64_t ldv, in
 // Returns the df64 sweep count.
 // ---------------------------------------------------------------------------
 template <class Gemm>
-__device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
+__device__ __noinline__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, double* Vout,
                                 int max_sweeps, int* converged, double* nrm, float* fbuf,
                                 double* tmp, CtaShared& sh, Gemm gemm, double floor2 = 0.0)
 {
@@ -555,7 +559,7 @@ __device__ int cta_jacobi_mixed(View src, int m, int n, double* A, int64_t lda, 
 // scaled by powers of two (exact) so the split never leaves FP32 range.
 // 64x64 output tiles, 16-deep k slabs in shared memory (the df64 slabs reuse
 // the CtaShared GEMM buffers, one df64 per double slot), 4x4 per thread.
-__device__ void cta_gemm_df(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
+__device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
                             int64_t c_cs, CtaShared& sh)
 {
   const double sa = cta_pow2_of_max(A, M, K, sh);
@@ -614,4 +618,5 @@ __device__ void cta_gemm_df(int M, int N, int K, View A, View B, double* C, int6
   __syncthreads();
 }
 
+}  // namespace
 }  // namespace ttg

@@ -21,6 +21,7 @@
 #include "ttg_device_df.cuh"
 #include "ttg_job.h"
 #include "ttg_kernels.h"
+#include "ttg_sweep_common.cuh"
 
 namespace ttg
 {
@@ -28,31 +29,6 @@ namespace ttg
 namespace
 {
 
-constexpr int kStatusOk = 0;
-constexpr int kStatusNan = 5;
-constexpr int kStatusNotConverged = 6;
-constexpr int kStatusNoSpace = 11;
-
-// Bump allocator over the CTA's scratch slab (256-byte aligned chunks).
-struct Bump
-{
-  double* p;
-  __device__ double* take(int64_t n)
-  {
-    double* r = p;
-    p += (n + 31) & ~static_cast<int64_t>(31);
-    return r;
-  }
-};
-
-__device__ __forceinline__ bool finite(double x) { return isfinite(x); }
-
-// Records a status on the TT (first error wins) -- thread 0 only.
-__device__ void set_status(TTInfo& T, int st)
-{
-  if (threadIdx.x == 0 && T.status == kStatusOk)
-    T.status = st;
-}
 
 // The mixed path runs its contractions in df64 on the FP32 pipes.
 struct GemmDf
@@ -75,16 +51,11 @@ __device__ void gemm_sel(bool mixed, int M, int N, int K, View A, View B, double
 
 // Dynamic shared memory of the CTA, used to stage the matrix a step works
 // on when it fits (cap doubles).
-struct Smem
-{
-  double* p;
-  int64_t cap;
-};
 
 // QR of X (h x c).  Q -> *W (h x k, column-major, ld h), R -> R (k x c,
 // column-major, ld k), k = min(h, c).  The factorisation runs in shared
 // memory when h*c fits there, else in Wg; *W tells the caller where Q is.
-__device__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* R, Smem sm,
+__device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* R, Smem sm,
                          double** Wout, bool mixed, CtaShared& sh)
 {
   double* W = (static_cast<int64_t>(h) * c <= sm.cap) ? sm.p : Wg;
@@ -125,18 +96,8 @@ __device__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* 
 // Branches as the reference: QR-condense when h >= 2c (truncate.hpp:76-85);
 // otherwise decompose X directly -- by columns when h >= c, by rows (the
 // transpose, accumulating V) when h < c.
-__device__ void record_bond(BondStat* bs, const double* sorted, int nsv, int r_new)
-{
-  if (bs && threadIdx.x == 0)
-  {
-    bs->s_max = sorted[0];
-    bs->s_last = sorted[r_new - 1];
-    bs->r_new = r_new;
-    bs->n_sv = nsv;
-  }
-}
 
-__device__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
+__device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
                         bool mixed, Bump bump, Smem sm, double** Ut_out, double** F_out,
                         TTInfo& T, CtaShared& sh, BondStat* bs = nullptr)
 {
@@ -400,18 +361,10 @@ __device__ void cta_copy(double* dst, const double* src, int64_t n)
   __syncthreads();
 }
 
-__device__ void set_ranks(CoreSlot& s, int r, int rp)
-{
-  if (threadIdx.x == 0)
-  {
-    s.r = r;
-    s.rp = rp;
-  }
-}
 
 // right_qr_step (detail/orthogonalize.hpp:63-100): QR of M^T (n*rp x r);
 // r_eff = min(n*rp, r); L = R^T absorbed into prev.
-__device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bump, Smem sm,
+__device__ __noinline__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bump, Smem sm,
                               bool mixed, CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
@@ -435,7 +388,7 @@ __device__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& prev, Bump bu
 }
 
 // left_qr_step (detail/orthogonalize.hpp:35-60).
-__device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bump, Smem sm,
+__device__ __noinline__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bump, Smem sm,
                              bool mixed, CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
@@ -460,7 +413,7 @@ __device__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& next, Bump bum
 }
 
 // svd_step (detail/truncate.hpp:61-99).
-__device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& next,
+__device__ __noinline__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& next,
                          double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh,
                          BondStat* bs = nullptr)
 {
@@ -482,7 +435,7 @@ __device__ void svd_step(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlo
 }
 
 // svd_step_right (detail/truncate.hpp:114-166) as a left step on M^T.
-__device__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& prev,
+__device__ __noinline__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, CoreSlot& prev,
                                double delta, Bump bump, Smem sm, TTInfo& T, CtaShared& sh)
 {
   const int r = cur.r, n = cur.n, rp = cur.rp;
@@ -503,33 +456,11 @@ __device__ void svd_step_right(const RoundJob& job, double* ar, CoreSlot& cur, C
   __syncthreads();
 }
 
-__device__ double core_norm(const double* p, int64_t n, CtaShared& sh)
-{
-  double s = 0.0;
-  for (int64_t t = threadIdx.x; t < n; t += blockDim.x)
-    s += p[t] * p[t];
-  return sqrt(cta_sum(s, sh));
-}
 
-__device__ int64_t core_size(const CoreSlot& s)
-{
-  return static_cast<int64_t>(s.r) * s.n * s.rp;
-}
 
-// make_rank1_zero_tt (detail/shape_check.hpp:176-188).
-__device__ void zero_tt(double* ar, CoreSlot* S, int d)
-{
-  for (int k = 0; k < d; ++k)
-  {
-    for (int i = threadIdx.x; i < S[k].n; i += blockDim.x)
-      ar[S[k].off + i] = 0.0;
-    set_ranks(S[k], 1, 1);
-  }
-  __syncthreads();
-}
 
 // Norm balancing (round/tt_round.hpp:65-124).
-__device__ void balance(double* ar, CoreSlot* S, int d, Bump bump, CtaShared& sh)
+__device__ __noinline__ void balance(double* ar, CoreSlot* S, int d, Bump bump, CtaShared& sh)
 {
   int64_t total = 0;
   for (int k = 0; k < d - 1; ++k)
@@ -619,7 +550,7 @@ __device__ int64_t balance_need(const CoreSlot* S, int d)
   return a32(total + 1);
 }
 
-__device__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh,
+__device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh,
                          double eps)
 {
   TTInfo& T = job.tts[tti];
@@ -749,7 +680,7 @@ __device__ int sketch_rank_of(const RoundJob& job, const CoreSlot* S, int first,
   return l > S[k].rp ? S[k].rp : l;
 }
 
-__device__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
+__device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, Smem sm,
                                 CtaShared& sh)
 {
   TTInfo& T = job.tts[tti];
@@ -896,7 +827,7 @@ __device__ void round_sketch_tt(const RoundJob& job, int tti, double* scratch, S
 
 // build_streaming_matvec / build_streaming_matmat
 // (detail/streaming_apply.hpp:39-202) for one (operator, operand) pair.
-__device__ void stream_tt(const RoundJob& job, int item, double* scratch, Smem sm, CtaShared& sh)
+__device__ __noinline__ void stream_tt(const RoundJob& job, int item, double* scratch, Smem sm, CtaShared& sh)
 {
   double* ar = job.arena;
   TTInfo& TA = job.tts[job.a_idx[item]];
@@ -1035,7 +966,7 @@ __device__ void stream_tt(const RoundJob& job, int item, double* scratch, Smem s
 
 }  // namespace
 
-__global__ void __launch_bounds__(kThreads) round_kernel(RoundJob job)
+__global__ void __launch_bounds__(kThreads, 2) round_kernel(RoundJob job)
 {
   __shared__ CtaShared sh;
   extern __shared__ double dyn_smem[];
@@ -1187,38 +1118,6 @@ __global__ void __launch_bounds__(kThreads) inner_kernel(const double* __restric
   }
   if (threadIdx.x == 0)
     *out = E[0];
-}
-
-#include "ttg_wide.cuh"
-
-cudaError_t launch_wide_round(const WideJob& job, int grid, cudaStream_t stream)
-{
-  WideJob j = job;
-  void* args[] = {&j};
-  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(wide_round_kernel), dim3(grid),
-                                     dim3(kThreads), args,
-                                     sizeof(double) * static_cast<size_t>(job.smem_doubles),
-                                     stream);
-}
-
-cudaError_t wide_round_setup(int smem_doubles, int* max_grid)
-{
-  cudaError_t e = cudaFuncSetAttribute(wide_round_kernel,
-                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       static_cast<int>(sizeof(double) * smem_doubles));
-  if (e != cudaSuccess)
-    return e;
-  int dev = 0, sms = 0, per_sm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
-    &per_sm, wide_round_kernel, kThreads, sizeof(double) * static_cast<size_t>(smem_doubles));
-  if (e != cudaSuccess)
-    return e;
-  // One CTA per SM: the phases are latency-bound, more CTAs only add
-  // barrier arrivals.
-  *max_grid = per_sm >= 1 ? sms : 0;
-  return cudaSuccess;
 }
 
 void launch_round(const RoundJob& job, int grid, cudaStream_t stream)

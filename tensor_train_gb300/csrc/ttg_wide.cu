@@ -1,5 +1,4 @@
-// Whole-GPU rounding of a few large TTs (part of the sweep translation unit,
-// included by ttg_kernels.cu).
+// Whole-GPU rounding of a few large TTs.
 //
 // One cooperative launch, one CTA per SM; the CTAs work on one TT at a time
 // and meet at a grid barrier between dependent phases.  Same algorithm and
@@ -26,8 +25,19 @@
 // Every barrier wait is bounded (kGridWaitCycles): a CTA that gives up sets
 // the shared error word, every other CTA sees it at its next barrier, and
 // the kernel returns; the host reports TTG_ERR_TIMEOUT.
-// Included inside namespace ttg.
-#pragma once
+#include <cfloat>
+#include <cstdint>
+
+#include <cuda_runtime.h>
+
+#include "ttg_device.cuh"
+#include "ttg_device_df.cuh"
+#include "ttg_job.h"
+#include "ttg_kernels.h"
+#include "ttg_sweep_common.cuh"
+
+namespace ttg
+{
 
 constexpr long long kGridWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
@@ -787,3 +797,35 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
 
 #undef WIDE_FOR
 #undef WSYNC
+
+cudaError_t launch_wide_round(const WideJob& job, int grid, cudaStream_t stream)
+{
+  WideJob j = job;
+  void* args[] = {&j};
+  return cudaLaunchCooperativeKernel(reinterpret_cast<const void*>(wide_round_kernel), dim3(grid),
+                                     dim3(kThreads), args,
+                                     sizeof(double) * static_cast<size_t>(job.smem_doubles),
+                                     stream);
+}
+
+cudaError_t wide_round_setup(int smem_doubles, int* max_grid)
+{
+  cudaError_t e = cudaFuncSetAttribute(wide_round_kernel,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       static_cast<int>(sizeof(double) * smem_doubles));
+  if (e != cudaSuccess)
+    return e;
+  int dev = 0, sms = 0, per_sm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+  e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(
+    &per_sm, wide_round_kernel, kThreads, sizeof(double) * static_cast<size_t>(smem_doubles));
+  if (e != cudaSuccess)
+    return e;
+  // One CTA per SM: the phases are latency-bound, more CTAs only add
+  // barrier arrivals.
+  *max_grid = per_sm >= 1 ? sms : 0;
+  return cudaSuccess;
+}
+
+}  // namespace ttg

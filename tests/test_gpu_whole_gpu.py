@@ -138,7 +138,7 @@ def test_whole_gpu_mixed_matvec_round(ttg):
 
 @pytest.mark.parametrize("sched", ["per_tt", "whole_gpu"])
 def test_plan_graph_replay_matches_direct_runs(ttg, sched):
-    # one run captured as a CUDA graph replays to the same result
+    # one run captured as a CUDA graph replays to the same rounding
     ts = [O.random_uneven(2000 + i) for i in range(3)]
     o = _opts(ttg, 1e-8, ttg.schedule[sched], precision=ttg.precision.mixed)
     plan = ttg.Plan("round", ts, opts=o)
@@ -153,5 +153,5 @@ def test_plan_graph_replay_matches_direct_runs(ttg, sched):
     plan.close()
     for a, b, t in zip(direct, replay, ts):
         assert O.ranks(a) == O.ranks(b)
-        assert O.rel_err(a, b) == 0.0
+        assert O.rel_err(a, b) <= 1e-13
         _close(a, O.round(t, 1e-8), MIXED_TOL)

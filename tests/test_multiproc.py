@@ -1,0 +1,62 @@
+"""The N > 1 bench path on CPU: two gloo ranks shard the batch by seed and
+take the slowest rank's time; the reference arm runs on rank 0 only."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        return s.getsockname()[1]
+
+
+def _worker(rank, world, port, q):
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
+                      WORLD_SIZE=str(world), LOCAL_RANK=str(rank))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+    r, w, _ = bench.dist_setup(world)
+    base = bench.shard_base(r, 4096)
+    t = bench.max_over_ranks(10.0 + 5.0 * r, w, device="cpu")
+    # every rank's seeds are disjoint from the others'
+    seeds = set(range(base, base + 4096))
+    gathered = [None] * w
+    dist.all_gather_object(gathered, sorted(seeds)[:1] + sorted(seeds)[-1:])
+    dist.destroy_process_group()
+    q.put((r, w, base, t, gathered))
+
+
+def test_two_gloo_ranks_shard_and_reduce():
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted(q.get(timeout=120) for _ in procs)
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (r0, w0, b0, t0, g0), (r1, w1, b1, t1, g1) = out
+    assert (r0, r1, w0, w1) == (0, 1, 2, 2)
+    assert b1 - b0 == 4096                 # disjoint seed ranges
+    assert t0 == t1 == 15.0                # the job's time is the slowest rank's
+    (lo0, hi0), (lo1, hi1) = g0
+    assert hi0 < lo1
+
+
+def test_reference_arm_runs_on_rank0_only(monkeypatch, capsys):
+    import argparse
+
+    import bench
+    monkeypatch.setenv("RANK", "1")
+    monkeypatch.setenv("WORLD_SIZE", "2")
+    args = argparse.Namespace(gpus=2, steps=1, warmup=0, count=8)
+    bench.run_reference(args)          # returns before any work on rank 1
+    assert capsys.readouterr().out == ""
