@@ -433,6 +433,8 @@ class Plan:
         v = c.value
         if v in (1, 2):
             return f"per_tt x{v}"
+        if v > 1000:
+            return f"whole_gpu b={v - 1100} tensor_cores"
         if v > 100:
             return f"whole_gpu b={v - 100}"
         return ""

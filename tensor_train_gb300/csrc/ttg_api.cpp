@@ -487,6 +487,13 @@ int32_t setup_wide(ttg_plan& P)
   j.part = reinterpret_cast<double*>(b + opart);
   j.umax = reinterpret_cast<unsigned long long*>(b + oumax);
   j.mixed = P.opts.precision == TTG_PREC_MIXED ? 1 : 0;
+  // Sliced-BF16 tensor-core contractions (mixed path only): measured slower
+  // than the FP64 tiles on these latency-bound sweeps, so off unless
+  // TTG_WIDE_TENSOR_CORES=1 or the autotuner picks them.
+  {
+    const char* e = std::getenv("TTG_WIDE_TENSOR_CORES");
+    j.tc = (j.mixed && e && e[0] == '1') ? 1 : 0;
+  }
   j.tau = reinterpret_cast<double*>(b + otau);
   j.sig = reinterpret_cast<double*>(b + osig);
   j.sorted = reinterpret_cast<double*>(b + osorted);
@@ -1052,15 +1059,15 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   const int items = static_cast<int>(P->order.size());
   struct Cand
   {
-    int code;  // 1/2: per TT, CTAs per SM; 100 + b: whole GPU with block width b
+    int code;  // 1/2: per TT, CTAs per SM; 100 + b (+ 1000 with tensor cores): whole GPU
     bool wide;
-    int grid, smem, jblock;
+    int grid, smem, jblock, tc;
   };
   std::vector<Cand> cands;
   const int g1 = std::max(1, std::min(items, sms)), g2 = std::max(1, std::min(items, 2 * sms));
-  cands.push_back({1, false, g1, kSmemOnePerSm, P->wjob.jblock});
+  cands.push_back({1, false, g1, kSmemOnePerSm, P->wjob.jblock, P->wjob.tc});
   if (g2 > g1)
-    cands.push_back({2, false, g2, kSmemTwoPerSm, P->wjob.jblock});
+    cands.push_back({2, false, g2, kSmemTwoPerSm, P->wjob.jblock, P->wjob.tc});
   const bool can_wide = P->wide_grid > 0 && P->wjob.W != nullptr;
   if (can_wide)
   {
@@ -1071,12 +1078,13 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
         const CoreSlot& c = P->slots[P->tts[t].first + k];
         c_max = std::max<int64_t>(c_max, std::max(c.r, c.rp));
       }
-    for (int b : {2, 4, 8})
-      if ((6 * c_max + 2) * b <= kSmemOnePerSm)
-        cands.push_back({100 + b, true, P->wide_grid, kSmemOnePerSm, b});
+    for (int tcv = 0; tcv <= P->wjob.mixed; ++tcv)
+      for (int b : {2, 4, 8})
+        if ((6 * c_max + 2) * b <= kSmemOnePerSm)
+          cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv});
   }
   const bool wide0 = P->wide;
-  const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock;
+  const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock, tc0 = P->wjob.tc;
   float best = 0.0f;
   int bi = -1;
   for (size_t i = 0; i < cands.size(); ++i)
@@ -1086,6 +1094,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->grid = c.grid;
     P->smem_doubles = c.smem;
     P->wjob.jblock = c.jblock;
+    P->wjob.tc = c.tc;
     float ms = 0.0f;
     for (int rep = 0; rep < 2; ++rep)  // warm, then timed
     {
@@ -1115,6 +1124,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->grid = grid0;
     P->smem_doubles = smem0;
     P->wjob.jblock = jb0;
+    P->wjob.tc = tc0;
     return TTG_OK;
   }
   const Cand& c = cands[static_cast<size_t>(bi)];
@@ -1122,6 +1132,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   P->grid = c.grid;
   P->smem_doubles = c.smem;
   P->wjob.jblock = c.jblock;
+  P->wjob.tc = c.tc;
   if (choice)
     *choice = c.code;
   return TTG_OK;

@@ -131,6 +131,7 @@ struct WideJob
   int max_sweeps;
   int jblock;          // Jacobi block width (columns)
   int mixed;           // 1: FP32 + df64 SVD sweeps
+  int tc;              // 1: contractions with K <= 512 on the tensor cores (sliced BF16)
   int64_t smem_doubles;
   double eps;
   double* W;           // core_max: reflectors

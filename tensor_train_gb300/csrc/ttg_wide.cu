@@ -34,6 +34,7 @@
 #include "ttg_device_df.cuh"
 #include "ttg_job.h"
 #include "ttg_kernels.h"
+#include "ttg_ozaki.cuh"
 #include "ttg_sweep_common.cuh"
 
 namespace ttg
@@ -95,6 +96,7 @@ struct WideSmem
 {
   double* p;
   int64_t cap;  // doubles
+  OzState* oz;  // TMEM accumulator and MMA barrier of this CTA (null: FP64 tiles only)
 };
 
 // dst[0..n) = src[0..n), spread over the grid.
@@ -105,14 +107,29 @@ __device__ void wide_copy(double* dst, const double* src, int64_t n)
     dst[t] = src[t];
 }
 
-// C = A B over the grid: 64x64 tiles, tile t on CTA t mod P.
-__device__ void wide_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
-                          int64_t c_cs, CtaShared& sh)
+// C = A B over the grid, tile t on CTA t mod P: 128x64 sliced-BF16 tiles
+// on the tensor cores (FP64-accurate, oz_tile) when the job allows them and
+// K <= 512, else 64x64 FP64 tiles.  Returns false if a tensor-core wait
+// timed out (the grid error word is set).
+__device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View B, double* C,
+                          int64_t c_rs, int64_t c_cs, WideSmem sm, CtaShared& sh)
 {
+  if (job.tc && sm.oz && K <= 512 && static_cast<int64_t>(kOzSmemBytes) <= sm.cap * 8)
+  {
+    const int tm = (M + kOzM - 1) / kOzM, tn = (N + kOzN - 1) / kOzN;
+    bool ok = true;
+    for (int t = blockIdx.x; t < tm * tn && ok; t += gridDim.x)
+      ok = oz_tile((t / tn) * kOzM, (t % tn) * kOzN, M, N, K, A, B, C, c_rs, c_cs,
+                   reinterpret_cast<uint8_t*>(sm.p), *sm.oz, sh);
+    if (!ok && threadIdx.x == 0)
+      atomicExch(&job.bar->err, 1);
+    return ok;
+  }
   const int tm = (M + 63) / 64, tn = (N + 63) / 64;
   for (int t = blockIdx.x; t < tm * tn; t += gridDim.x)
     cta_gemm_tile((t / tn) * 64, (t % tn) * 64, M, N, K, A, B, C, c_rs, c_cs, sh);
   __syncthreads();
+  return true;
 }
 
 // Householder QR of X (h x c), column-distributed.  Reflector tails go to
@@ -417,18 +434,21 @@ __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool 
   {
     double* Vin = it == 0 ? Vd : job.V;
     double* Vout = it == 0 ? job.V : Vd;
-    wide_gemm(q, q, q, View{Vin, q, 1}, View{Vin, 1, q}, job.F, 1, q, sh);
+    if (!wide_gemm(job, q, q, q, View{Vin, q, 1}, View{Vin, 1, q}, job.F, 1, q, sm, sh))
+      return false;
     WSYNC();
     WIDE_FOR(e, qq)
     job.F[e] = ((e % q == e / q) ? 1.5 : 0.0) - 0.5 * job.F[e];
     WSYNC();
-    wide_gemm(q, q, q, View{Vin, 1, q}, View{job.F, 1, q}, Vout, 1, q, sh);
+    if (!wide_gemm(job, q, q, q, View{Vin, 1, q}, View{job.F, 1, q}, Vout, 1, q, sm, sh))
+      return false;
     WSYNC();
   }
   // The result is in Vd (T2); V takes it.
   wide_copy(job.V, Vd, qq);
   WSYNC();
-  wide_gemm(p, q, q, src, View{job.V, 1, q}, job.A, 1, p, sh);
+  if (!wide_gemm(job, p, q, q, src, View{job.V, 1, q}, job.A, 1, p, sm, sh))
+    return false;
   WSYNC();
   // df64 polish on A / 2^e, 2^e <= max|A| < 2^(e+1) (bit-pattern max).
   {
@@ -615,7 +635,8 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
     // core_k <- Q^T (Q column-major w x kk is the core's row-major layout);
     // prev (hp x kk) = left_unfold(prev) R^T.
     wide_apply_q(job, w, kk, nullptr, 0, kk, cs, 1, w, true, sm, sh);
-    wide_gemm(hp, kk, r, View{ps, r, 1}, View{job.R, kk, 1}, job.Pb, kk, 1, sh);
+    if (!wide_gemm(job, hp, kk, r, View{ps, r, 1}, View{job.R, kk, 1}, job.Pb, kk, 1, sm, sh))
+      return false;
     WSYNC();
     wide_copy(ps, job.Pb, static_cast<int64_t>(hp) * kk);
     if (lead)
@@ -687,7 +708,8 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
       }
       WSYNC();
       // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
-      wide_gemm(r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sh);
+      if (!wide_gemm(job, r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sm, sh))
+        return false;
       wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
       WSYNC();
     }
@@ -717,7 +739,8 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
       }
       WSYNC();
       // F = U^T X.
-      wide_gemm(r_new, c, h, View{job.Ub, h, 1}, X, job.F, c, 1, sh);
+      if (!wide_gemm(job, r_new, c, h, View{job.Ub, h, 1}, X, job.F, c, 1, sm, sh))
+        return false;
       WSYNC();
     }
     else
@@ -760,7 +783,8 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
         T.sweeps = sweeps;
     }
     // next (r_new x wn) = F right_unfold(next); core_k <- U (row-major).
-    wide_gemm(r_new, wn, c, View{job.F, c, 1}, View{ns, wn, 1}, job.Pb, wn, 1, sh);
+    if (!wide_gemm(job, r_new, wn, c, View{job.F, c, 1}, View{ns, wn, 1}, job.Pb, wn, 1, sm, sh))
+      return false;
     WSYNC();
     wide_copy(ns, job.Pb, static_cast<int64_t>(r_new) * wn);
     {
@@ -789,10 +813,35 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
 {
   extern __shared__ double dyn_smem[];
   __shared__ CtaShared sh;
-  const WideSmem sm{dyn_smem, job.smem_doubles};
+  __shared__ uint32_t tmem_base;
+  __shared__ __align__(8) uint64_t mbar;
+  OzState oz{0u, &mbar, 0u};
+  if (job.tc)
+  {
+    // One CTA per SM: the whole TMEM (512 columns) is free for this CTA.
+    if ((threadIdx.x >> 5) == 0)
+      tc::tmem_alloc(&tmem_base, kOzTmemCols);
+    if (threadIdx.x == 0)
+      tc::mbar_init(&mbar, 1);
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    oz.tmem = tmem_base;
+  }
+  const WideSmem sm{dyn_smem, job.smem_doubles, job.tc ? &oz : nullptr};
   for (int i = 0; i < job.ntt; ++i)
     if (!wide_round_tt(job, job.order ? job.order[i] : i, sm, sh))
-      return;
+      break;
+  if (job.tc)
+  {
+    tc::fence_before_sync();
+    __syncthreads();
+    if ((threadIdx.x >> 5) == 0)
+    {
+      tc::fence_after_sync();
+      tc::tmem_dealloc(oz.tmem, kOzTmemCols);
+    }
+  }
 }
 
 #undef WIDE_FOR

@@ -155,3 +155,30 @@ def test_plan_graph_replay_matches_direct_runs(ttg, sched):
         assert O.ranks(a) == O.ranks(b)
         assert O.rel_err(a, b) <= 1e-13
         _close(a, O.round(t, 1e-8), MIXED_TOL)
+
+
+@pytest.mark.parametrize("n,r,seed", [(4, 40, 31), (8, 48, 21)])
+def test_whole_gpu_mixed_tensor_core_contractions(ttg, monkeypatch, n, r, seed):
+    # contractions as sliced-BF16 tcgen05 tiles (5 slices, FP32 accumulation
+    # in TMEM, FP64 epilogue): ~1e-12 per contraction
+    monkeypatch.setenv("TTG_WIDE_TENSOR_CORES", "1")
+    a = O.random([n] * 7, r, seed, fan_in_scale=True)
+    b = O.random([n] * 7, r, seed + 1, fan_in_scale=True)
+    t = O.add(a, b)
+    y = ttg.round(t, _opts(ttg, 1e-8, ttg.schedule.whole_gpu, precision=ttg.precision.mixed))
+    _close(y, O.round(t, 1e-8), 1e-9)
+
+
+def test_autotune_keeps_parity(ttg):
+    ts = [O.random_uneven(3000 + i) for i in range(3)]
+    for prec in (ttg.precision.fp64, ttg.precision.mixed):
+        plan = ttg.Plan("round", ts, opts=_opts(ttg, 1e-8, ttg.schedule.auto, precision=prec))
+        plan.upload()
+        choice = plan.autotune()
+        assert choice.startswith("per_tt") or choice.startswith("whole_gpu")
+        plan.graph(True)
+        plan.run()
+        ys = plan.download()
+        plan.close()
+        for y, t in zip(ys, ts):
+            _close(y, O.round(t, 1e-8), TOL if prec == ttg.precision.fp64 else MIXED_TOL)
