@@ -242,11 +242,11 @@ int32_t ttg_plan_upload(ttg_plan* plan, void* stream);
  * the sweep on it.  Idempotent: repeated runs give the same result. */
 int32_t ttg_plan_run(ttg_plan* plan, void* stream);
 /* Autotuner: times the plan's launch configurations on the plan itself
- * (per-TT schedule: 1 or 2 CTAs per SM, i.e. 200 or 92 KB of shared staging
- * per CTA; whole-GPU schedule: Jacobi block widths 2/4/8, and the per-TT
+ * (per-TT schedule: 1, 2, 3 or 4 CTAs per SM, i.e. 200, 92, 56 or 38 KB of
+ * shared staging and 128, 128, 85 or 64 registers per thread; whole-GPU schedule: Jacobi block widths 2/4/8, and the per-TT
  * schedule as a contender; on the mixed path also with and without the
  * sliced-BF16 tensor-core contractions) and keeps the fastest.  *choice
- * (optional): 1 or 2 = per TT with that many CTAs per SM, 100 + b = whole
+ * (optional): 1-4 = per TT with that many CTAs per SM, 100 + b = whole
  * GPU with block width b (+1000 with tensor-core contractions), 0 = nothing
  * to tune.  Synchronises `stream`; drops a captured
  * graph (capture again afterwards). */

@@ -431,7 +431,7 @@ class Plan:
         c = C.c_int32()
         _check(lib().ttg_plan_autotune(self.h, C.c_void_p(stream), C.byref(c)), "plan_autotune")
         v = c.value
-        if v in (1, 2):
+        if v in (1, 2, 3, 4):
             return f"per_tt x{v}"
         if v > 1000:
             return f"whole_gpu b={v - 1100} tensor_cores"

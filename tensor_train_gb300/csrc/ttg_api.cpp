@@ -266,6 +266,8 @@ struct ttg_plan
   int64_t arena_doubles = 0;
   int64_t scratch_stride = 0;
   int grid = 1;
+  int cps = 2;          // resident CTAs per SM of the sweep kernel instantiation
+  int scratch_ctas = 1; // CTAs the scratch slabs were allocated for
   int smem_doubles = 0;
   // products computed on the device before the sweep (naive apply-round):
   struct Apply
@@ -405,6 +407,8 @@ double est_cost(const Shape& s)
 // is larger than the SM count, one CTA gets ~200 KB otherwise.
 constexpr int kSmemTwoPerSm = 11776;  // 92 KB
 constexpr int kSmemOnePerSm = 25600;  // 200 KB
+constexpr int kSmemThreePerSm = 7168;  // 56 KB
+constexpr int kSmemFourPerSm = 4864;   // 38 KB
 
 // Whole-GPU schedule: chosen for round jobs (gauge none, method svd) by
 // the options, or automatically for at most 4 TTs with a bond rank >= 64.
@@ -515,7 +519,24 @@ int32_t layout_and_alloc(ttg_plan& P)
   if (optin != cudaSuccess)
     return fail(TTG_ERR_CUDA, std::string("round kernel shared-memory opt-in: ") +
                                   cudaGetErrorString(optin));
-  P.smem_doubles = P.grid > std::max(device().sms, 1) ? kSmemTwoPerSm : kSmemOnePerSm;
+  const int sms = std::max(device().sms, 1);
+  P.smem_doubles = P.grid > sms ? kSmemTwoPerSm : kSmemOnePerSm;
+  P.cps = P.grid > sms ? 2 : 1;
+  // Large batches get scratch for up to 4 CTAs per SM (autotuner candidates)
+  // and start at 4 per SM, the autotuner's pick on the uneven 4096-TT batch
+  // (the sweeps are latency-bound: more resident TTs hide more of it).
+  P.scratch_ctas = P.grid;
+  if (static_cast<int64_t>(P.order.size()) > 2LL * sms && P.job_kind >= 0)
+  {
+    P.scratch_ctas = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(P.order.size()),
+                                                        4LL * sms));
+    if (static_cast<int64_t>(P.order.size()) >= 4LL * sms)
+    {
+      P.grid = P.scratch_ctas;
+      P.cps = 4;
+      P.smem_doubles = kSmemFourPerSm;
+    }
+  }
   size_t o = 0;
   P.off_arena = o;
   o = align256(o + sizeof(double) * static_cast<size_t>(P.arena_doubles));
@@ -541,7 +562,8 @@ int32_t layout_and_alloc(ttg_plan& P)
   P.off_stats = o;
   o = align256(o + (P.opts.bond_stats ? sizeof(BondStat) * P.slots.size() : 0));
   P.off_scratch = o;
-  o = align256(o + sizeof(double) * static_cast<size_t>(P.scratch_stride) * P.grid);
+  o = align256(o + sizeof(double) * static_cast<size_t>(P.scratch_stride) *
+                       static_cast<size_t>(std::max(P.grid, P.scratch_ctas)));
   P.total_bytes = o;
   TTG_CUDA(P.dev.ensure(P.total_bytes));
   TTG_CUDA(P.host.ensure(P.prefix_bytes));
@@ -758,7 +780,7 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
       TTG_CUDA(launch_wide_round(P.wjob, P.wide_grid, st));
     }
     else
-      launch_round(make_job(P), P.grid, st);
+      launch_round(make_job(P), P.grid, P.cps, st);
     TTG_CUDA(record_event(P.evk1, st));
     P.kernel_timed = true;
     g_launches += 1;
@@ -1061,13 +1083,18 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   {
     int code;  // 1/2: per TT, CTAs per SM; 100 + b (+ 1000 with tensor cores): whole GPU
     bool wide;
-    int grid, smem, jblock, tc;
+    int grid, smem, jblock, tc, cps;
   };
   std::vector<Cand> cands;
   const int g1 = std::max(1, std::min(items, sms)), g2 = std::max(1, std::min(items, 2 * sms));
-  cands.push_back({1, false, g1, kSmemOnePerSm, P->wjob.jblock, P->wjob.tc});
+  cands.push_back({1, false, g1, kSmemOnePerSm, P->wjob.jblock, P->wjob.tc, 1});
   if (g2 > g1)
-    cands.push_back({2, false, g2, kSmemTwoPerSm, P->wjob.jblock, P->wjob.tc});
+    cands.push_back({2, false, g2, kSmemTwoPerSm, P->wjob.jblock, P->wjob.tc, 2});
+  const int g3 = std::max(1, std::min(items, 3 * sms)), g4 = std::max(1, std::min(items, 4 * sms));
+  if (g3 > g2 && g3 <= P->scratch_ctas)
+    cands.push_back({3, false, g3, kSmemThreePerSm, P->wjob.jblock, P->wjob.tc, 3});
+  if (g4 > g3 && g4 <= P->scratch_ctas)
+    cands.push_back({4, false, g4, kSmemFourPerSm, P->wjob.jblock, P->wjob.tc, 4});
   const bool can_wide = P->wide_grid > 0 && P->wjob.W != nullptr;
   if (can_wide)
   {
@@ -1081,10 +1108,11 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     for (int tcv = 0; tcv <= P->wjob.mixed; ++tcv)
       for (int b : {2, 4, 8})
         if ((6 * c_max + 2) * b <= kSmemOnePerSm)
-          cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv});
+          cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv, 1});
   }
   const bool wide0 = P->wide;
-  const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock, tc0 = P->wjob.tc;
+  const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock, tc0 = P->wjob.tc,
+            cps0 = P->cps;
   float best = 0.0f;
   int bi = -1;
   for (size_t i = 0; i < cands.size(); ++i)
@@ -1095,6 +1123,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->smem_doubles = c.smem;
     P->wjob.jblock = c.jblock;
     P->wjob.tc = c.tc;
+    P->cps = c.cps;
     float ms = 0.0f;
     for (int rep = 0; rep < 2; ++rep)  // warm, then timed
     {
@@ -1125,6 +1154,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->smem_doubles = smem0;
     P->wjob.jblock = jb0;
     P->wjob.tc = tc0;
+    P->cps = cps0;
     return TTG_OK;
   }
   const Cand& c = cands[static_cast<size_t>(bi)];
@@ -1133,6 +1163,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   P->smem_doubles = c.smem;
   P->wjob.jblock = c.jblock;
   P->wjob.tc = c.tc;
+  P->cps = c.cps;
   if (choice)
     *choice = c.code;
   return TTG_OK;

@@ -966,7 +966,10 @@ __device__ __noinline__ void stream_tt(const RoundJob& job, int item, double* sc
 
 }  // namespace
 
-__global__ void __launch_bounds__(kThreads, 2) round_kernel(RoundJob job)
+// MinBlocks CTAs of 256 threads resident per SM (the register cap follows:
+// 128, 85 or 64 per thread); the autotuner picks the instantiation.
+template <int MinBlocks>
+__global__ void __launch_bounds__(kThreads, MinBlocks) round_kernel(RoundJob job)
 {
   __shared__ CtaShared sh;
   extern __shared__ double dyn_smem[];
@@ -1120,16 +1123,27 @@ __global__ void __launch_bounds__(kThreads) inner_kernel(const double* __restric
     *out = E[0];
 }
 
-void launch_round(const RoundJob& job, int grid, cudaStream_t stream)
+void launch_round(const RoundJob& job, int grid, int ctas_per_sm, cudaStream_t stream)
 {
   const size_t smem = sizeof(double) * static_cast<size_t>(job.smem_doubles);
-  round_kernel<<<grid, kThreads, smem, stream>>>(job);
+  if (ctas_per_sm >= 4)
+    round_kernel<4><<<grid, kThreads, smem, stream>>>(job);
+  else if (ctas_per_sm == 3)
+    round_kernel<3><<<grid, kThreads, smem, stream>>>(job);
+  else
+    round_kernel<2><<<grid, kThreads, smem, stream>>>(job);
 }
 
 cudaError_t round_smem_optin(int smem_doubles)
 {
-  return cudaFuncSetAttribute(round_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                              static_cast<int>(sizeof(double) * smem_doubles));
+  const int bytes = static_cast<int>(sizeof(double) * smem_doubles);
+  cudaError_t e = cudaFuncSetAttribute(round_kernel<2>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(round_kernel<3>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(round_kernel<4>, cudaFuncAttributeMaxDynamicSharedMemorySize, bytes);
+  return e;
 }
 
 void launch_apply_core(const double* A, const double* X, double* Y, int r, int m, int p, int rp,

@@ -10,7 +10,8 @@
 namespace ttg
 {
 
-void launch_round(const RoundJob& job, int grid, cudaStream_t stream);
+// ctas_per_sm: 1-2 (128 registers), 3 (85) or 4 (64): the instantiation.
+void launch_round(const RoundJob& job, int grid, int ctas_per_sm, cudaStream_t stream);
 // Whole-GPU rounding (cooperative launch, grid <= the value from setup).
 cudaError_t launch_wide_round(const WideJob& job, int grid, cudaStream_t stream);
 // Opt-in to the dynamic shared memory and the co-resident grid size.

@@ -290,7 +290,7 @@ int32_t ttg_round_noalloc(int32_t d, const int32_t* ranks, const int32_t* modes,
   job.eps = opts->eps;
   job.max_rank = opts->max_rank;
   job.max_sweeps = opts->max_sweeps > 0 ? opts->max_sweeps : 40;
-  launch_round(job, 1, st);
+  launch_round(job, 1, 1, st);
   noalloc_pack<<<1, 256, 0, st>>>(arena, slots, tt, d, out_dev, result);
   e = cudaGetLastError();
   if (e != cudaSuccess)
