@@ -1,5 +1,5 @@
 """CPU reference of the rank model's forward pass and mean-squared-error
-gradient -- TEST INFRASTRUCTURE ONLY (the checker of the GPU kernels).
+gradient -- TEST INFRASTRUCTURE ONLY (the expected values for the GPU kernels' tests).
 
 FP64 numpy, same parameter layout as the library: W1 (F x H) | b1 (H) |
 W2 (H x H) | b2 (H) | W3 (H) | b3 (1), row-major.

@@ -1,6 +1,6 @@
 """ctypes wrapper of the CPU oracle -- TEST INFRASTRUCTURE ONLY.
 
-Imported by tests/, by ``__graft_entry__.smoke()`` (as the checker) and by
+Imported by tests/, by ``__graft_entry__.smoke()`` (expected results) and by
 bench.py's CPU-baseline leg.  The product path never imports this module.
 
 A TT is a list of numpy float64 cores of shape (r, n, r'); a TT-matrix is a

@@ -1,7 +1,7 @@
 // CPU oracle for the TT-rounding hot path -- TEST INFRASTRUCTURE ONLY.
 //
 // A plain-C++20 FP64 restatement of the reference's algorithms, used by the
-// tests as the checker, by smoke() as the checker, and by bench.py as the
+// tests and by smoke() for the expected results, and by bench.py as the
 // timed CPU baseline.  The product (the CUDA library) never links, calls or
 // routes through this file.
 //

@@ -650,7 +650,7 @@ __device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scra
 //      with eps_r = sqrt(eps^2 - rel^2) ||X|| / ||Y||, which keeps the total
 //      within eps ||X|| and the per-bond threshold within 3% of the exact
 //      rounder's.  Otherwise the inputs are restored from the pristine copy
-//      and rounded exactly (the fallback that also judges the sketch).
+//      and rounded exactly (the fallback that also validates the sketch).
 // The acceptance test resolves ||X - Y||/||X|| down to ~1e-7 (FP64
 // cancellation of the two squared norms): meant for eps >= 1e-6.
 // ---------------------------------------------------------------------------
