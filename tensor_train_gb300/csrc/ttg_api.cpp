@@ -416,10 +416,40 @@ constexpr int kSmemFourPerSm = 4864;   // 38 KB
 int32_t setup_wide(ttg_plan& P)
 {
   P.wide = false;
-  if (P.job_kind != kJobRound || P.order.empty() || P.opts.schedule == TTG_SCHED_PER_TT)
+  const bool stream = P.job_kind == kJobStreamMatvec || P.job_kind == kJobStreamMatmat;
+  if ((P.job_kind != kJobRound && !stream) || P.order.empty() ||
+      P.opts.schedule == TTG_SCHED_PER_TT)
     return TTG_OK;
-  int64_t core_max = 1, c_max = 1, cols_max = 1;
-  for (int t : P.order)
+  // TTs whose cores the sweep touches: the rounded TTs, or every operand and
+  // output of the streaming items.
+  std::vector<int> swept;
+  if (stream)
+    for (int it : P.order)
+    {
+      swept.push_back(P.a_idx[it]);
+      swept.push_back(P.b_idx[it]);
+      swept.push_back(P.out_idx[it]);
+    }
+  else
+    swept = P.order;
+  int64_t core_max = 1, c_max = 1, cols_max = 1, s_max = 1, f_max = 1;
+  if (stream)
+    for (int it : P.order)
+    {
+      const TTInfo& ta = P.tts[P.a_idx[it]];
+      const TTInfo& tx = P.tts[P.b_idx[it]];
+      for (int k = 0; k < ta.d; ++k)
+      {
+        const CoreSlot& A = P.slots[ta.first + k];
+        const CoreSlot& X = P.slots[tx.first + k];
+        const int64_t a = A.r, b = A.rp, m = A.m, p = A.n / std::max(A.m, 1);
+        const int64_t sx = X.r, bx = X.rp, nout = X.n / std::max<int64_t>(p, 1);
+        const int64_t alpha = a * sx;  // the output's left bond never exceeds this
+        s_max = std::max({s_max, alpha * sx * a, alpha * sx * m * p * b, alpha * m * b * nout * bx});
+        f_max = std::max(f_max, (b * bx) * (b * bx));
+      }
+    }
+  for (int t : swept)
   {
     const TTInfo& ti = P.tts[t];
     int64_t cols = 0;
@@ -434,6 +464,8 @@ int32_t setup_wide(ttg_plan& P)
   }
   const bool want = P.opts.schedule == TTG_SCHED_WHOLE_GPU ||
                     (P.order.size() <= 4 && c_max >= 64);
+  if (stream)
+    core_max = std::max(core_max, s_max);
   if (!want)
     return TTG_OK;
   // Jacobi block pairs: (2 c_max rows + c_max V rows) x 2b columns + 2b norms.
@@ -463,7 +495,10 @@ int32_t setup_wide(ttg_plan& P)
                opart = take(8 * static_cast<size_t>(grid) + 8), oumax = take(8),
                otau = take(8 * c_max), osig = take(8 * c_max),
                osorted = take(8 * c_max), oord = take(4 * c_max), ocn = take(8 * (cols_max + 1)),
-               oival = take(64), orot = take(4 * ms), orel = take(4 * ms), obar = take(sizeof(GridBar));
+               oival = take(64), orot = take(4 * ms), orel = take(4 * ms), obar = take(sizeof(GridBar)),
+               oS1 = take(stream ? 8 * static_cast<size_t>(s_max) : 8),
+               oS2 = take(stream ? 8 * static_cast<size_t>(s_max) : 8),
+               oFs = take(stream ? 8 * static_cast<size_t>(f_max) : 8);
   TTG_CUDA(P.wdev.ensure(o));
   char* b = static_cast<char*>(P.wdev.p);
   char* d = static_cast<char*>(P.dev.p);
@@ -507,6 +542,13 @@ int32_t setup_wide(ttg_plan& P)
   j.sweep_rot = reinterpret_cast<unsigned int*>(b + orot);
   j.sweep_rel = reinterpret_cast<unsigned int*>(b + orel);
   j.bar = reinterpret_cast<GridBar*>(b + obar);
+  j.kind = P.job_kind;
+  j.a_idx = reinterpret_cast<const int32_t*>(d + P.off_aidx);
+  j.b_idx = reinterpret_cast<const int32_t*>(d + P.off_bidx);
+  j.out_idx = reinterpret_cast<const int32_t*>(d + P.off_oidx);
+  j.S1 = reinterpret_cast<double*>(b + oS1);
+  j.S2 = reinterpret_cast<double*>(b + oS2);
+  j.Fs = reinterpret_cast<double*>(b + oFs);
   j.bond_stats = P.opts.bond_stats ? reinterpret_cast<BondStat*>(d + P.off_stats) : nullptr;
   P.wide = true;
   P.wide_grid = grid;

@@ -132,6 +132,13 @@ struct WideJob
   int jblock;          // Jacobi block width (columns)
   int mixed;           // 1: FP32 + df64 SVD sweeps
   int tc;              // 1: contractions with K <= 512 on the tensor cores (sliced BF16)
+  int kind;            // kJobRound or kJobStreamMatvec / kJobStreamMatmat
+  const int* a_idx;    // streaming: operand and output TT of each item
+  const int* b_idx;
+  const int* out_idx;
+  double* S1;          // streaming: two contraction/permutation buffers
+  double* S2;
+  double* Fs;          // streaming: the running F factor
   int64_t smem_doubles;
   double eps;
   double* W;           // core_max: reflectors

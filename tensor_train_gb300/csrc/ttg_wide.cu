@@ -609,18 +609,13 @@ __device__ bool wide_balance(const WideJob& job, double* ar, CoreSlot* S, int d,
   return true;
 }
 
-// detail::round (gauge none) of TT tti over the whole grid.
-__device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShared& sh)
+// Right-to-left QR sweep (right_qr_step, detail/orthogonalize.hpp:63-100)
+// over cores d-1..1 of S.
+__device__ bool wide_right_orth(const WideJob& job, CoreSlot* S, int d, WideSmem sm,
+                                CtaShared& sh)
 {
-  TTInfo& T = job.tts[tti];
-  const int d = T.d;
-  CoreSlot* S = job.slots + T.first;
   double* ar = job.arena;
-  const int me = blockIdx.x;
-  const bool lead = (me == 0 && threadIdx.x == 0);
-  if (d <= 1)
-    return true;
-  // Right-to-left QR sweep (right_qr_step, detail/orthogonalize.hpp:63-100).
+  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
   for (int k = d - 1; k >= 1; --k)
   {
     const int r = S[k].r, n = S[k].n, rp = S[k].rp;
@@ -646,25 +641,173 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
     }
     WSYNC();
   }
-  const double nrm = core_norm(ar + S[0].off, core_size(S[0]), sh);
+  return true;
+}
+
+// Truncated SVD of X (h x c) over the grid, as left_svd of the per-TT
+// kernel (detail/truncate.hpp:61-99 branches): *r_new_out, U in job.Ub
+// (column-major, h x r_new), diag(s) V^T rows in job.F (row-major, r_new x
+// c).  X must not alias the work buffers (A, W, R, V, F, Ub, Pb, T1, T2).
+__device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double delta, TTInfo& T,
+                              BondStat* bs, WideSmem sm, CtaShared& sh, int* r_new_out)
+{
+  const int me = blockIdx.x;
+  const bool lead = (me == 0 && threadIdx.x == 0);
+  const int nsv = h < c ? h : c;
+  const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
+  int sweeps = 0, conv = 1, r_new = 1;
+  if (h >= 2 * c)
+  {
+    bool ok = true;
+    wide_qr(job, X, h, c, sm, sh, &ok);
+    if (!ok)
+      return false;
+    // A = R (c x c), then Jacobi.
+    wide_copy(job.A, job.R, static_cast<int64_t>(c) * c);
+    WSYNC();
+    if (job.mixed)
+    {
+      if (!wide_svd_mixed(job, View{job.R, 1, c}, c, c, false, floor2, sm, sh, &sweeps, &conv))
+        return false;
+    }
+    else if (!wide_jacobi<double>(job, job.A, c, c, c, nullptr, job.jblock, floor2,
+                                  kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
+      return false;
+    if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
+      return false;
+    r_new = job.ival[0];
+    // Uc (c x r_new) = A(:, ord) / s, into V.
+    for (int j = me; j < r_new; j += gridDim.x)
+    {
+      const double s = job.sorted[j];
+      const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
+      for (int i = threadIdx.x; i < c; i += blockDim.x)
+        job.V[i + static_cast<int64_t>(j) * c] = s > 0.0 ? a[i] / s : 0.0;
+    }
+    WSYNC();
+    // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
+    if (!wide_gemm(job, r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sm, sh))
+      return false;
+    wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
+    WSYNC();
+  }
+  else if (h >= c)
+  {
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+         e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+      job.A[e] = X(e % h, e / h);
+    WSYNC();
+    if (job.mixed)
+    {
+      if (!wide_svd_mixed(job, X, h, c, false, floor2, sm, sh, &sweeps, &conv))
+        return false;
+    }
+    else if (!wide_jacobi<double>(job, job.A, h, c, h, nullptr, job.jblock, floor2,
+                                  kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
+      return false;
+    if (!wide_truncate(job, job.A, h, c, h, delta, T, bs, sh))
+      return false;
+    r_new = job.ival[0];
+    for (int j = me; j < r_new; j += gridDim.x)
+    {
+      const double s = job.sorted[j];
+      const double* a = job.A + static_cast<int64_t>(job.ord[j]) * h;
+      for (int i = threadIdx.x; i < h; i += blockDim.x)
+        job.Ub[i + static_cast<int64_t>(j) * h] = s > 0.0 ? a[i] / s : 0.0;
+    }
+    WSYNC();
+    // F = U^T X.
+    if (!wide_gemm(job, r_new, c, h, View{job.Ub, h, 1}, X, job.F, c, 1, sm, sh))
+      return false;
+    WSYNC();
+  }
+  else
+  {
+    // Jacobi on X^T (c x h); V (h x h) accumulates and becomes U.
+    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+         e < static_cast<int64_t>(c) * h; e += stride)
+      job.A[e] = X(e / c, e % c);
+    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+         e < static_cast<int64_t>(h) * h; e += stride)
+      job.V[e] = (e % h == e / h) ? 1.0 : 0.0;
+    WSYNC();
+    if (job.mixed)
+    {
+      if (!wide_svd_mixed(job, transposed(X), c, h, true, floor2, sm, sh, &sweeps, &conv))
+        return false;
+    }
+    else if (!wide_jacobi<double>(job, job.A, c, h, c, job.V, job.jblock, floor2,
+                                  kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
+      return false;
+    if (!wide_truncate(job, job.A, c, h, c, delta, T, bs, sh))
+      return false;
+    r_new = job.ival[0];
+    for (int j = me; j < r_new; j += gridDim.x)
+    {
+      const int o = job.ord[j];
+      for (int i = threadIdx.x; i < h; i += blockDim.x)
+        job.Ub[i + static_cast<int64_t>(j) * h] = job.V[i + static_cast<int64_t>(o) * h];
+      for (int i = threadIdx.x; i < c; i += blockDim.x)
+        job.F[static_cast<int64_t>(j) * c + i] = job.A[i + static_cast<int64_t>(o) * c];
+    }
+    WSYNC();
+  }
+  if (lead)
+  {
+    if (!conv)
+      set_status(T, kStatusNotConverged);
+    if (sweeps > T.sweeps)
+      T.sweeps = sweeps;
+  }
+  *r_new_out = r_new;
+  return true;
+}
+
+// Norm, NaN and zero checks after the right-to-left sweep; *delta = the
+// truncation threshold.  Returns 0 to continue, 1 when the TT is finished
+// (NaN recorded or zeroed), -1 on a barrier failure.
+__device__ int wide_norm_step(const WideJob& job, TTInfo& T, CoreSlot* S, int d, double nrm,
+                              CtaShared& sh, double* delta)
+{
+  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
   if (lead)
     T.norm = nrm;
   if (!isfinite(nrm))
   {
-    if (me == 0)
+    if (blockIdx.x == 0)
       set_status(T, kStatusNan);
-    return true;
+    return 1;
   }
   if (nrm == 0.0)
   {
-    if (me == 0)
-      zero_tt(ar, S, d);
-    WSYNC();
-    return true;
+    if (blockIdx.x == 0)
+      zero_tt(job.arena, S, d);
+    return grid_sync(job.bar) ? 1 : -1;
   }
-  const double delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+  *delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
   if (lead)
-    T.delta = delta;
+    T.delta = *delta;
+  return 0;
+}
+
+// detail::round (gauge none) of TT tti over the whole grid.
+__device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShared& sh)
+{
+  TTInfo& T = job.tts[tti];
+  const int d = T.d;
+  CoreSlot* S = job.slots + T.first;
+  double* ar = job.arena;
+  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  if (d <= 1)
+    return true;
+  if (!wide_right_orth(job, S, d, sm, sh))
+    return false;
+  double delta = 0.0;
+  const int st = wide_norm_step(job, T, S, d, core_norm(ar + S[0].off, core_size(S[0]), sh), sh,
+                                &delta);
+  if (st != 0)
+    return st > 0;
   // Left-to-right truncated SVD sweep (svd_step, detail/truncate.hpp:61-99).
   for (int k = 0; k < d - 1; ++k)
   {
@@ -673,115 +816,10 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
     const int wn = S[k + 1].n * S[k + 1].rp;
     double* cs = ar + S[k].off;
     double* ns = ar + S[k + 1].off;
-    const View X{cs, c, 1};
-    const int nsv = h < c ? h : c;
-    const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
     BondStat* bs = job.bond_stats ? job.bond_stats + T.first + k : nullptr;
-    int sweeps = 0, conv = 1, r_new = 1;
-    if (h >= 2 * c)
-    {
-      bool ok = true;
-      wide_qr(job, X, h, c, sm, sh, &ok);
-      if (!ok)
-        return false;
-      // A = R (c x c), then Jacobi.
-      wide_copy(job.A, job.R, static_cast<int64_t>(c) * c);
-      WSYNC();
-      if (job.mixed)
-      {
-        if (!wide_svd_mixed(job, View{job.R, 1, c}, c, c, false, floor2, sm, sh, &sweeps, &conv))
-          return false;
-      }
-      else if (!wide_jacobi<double>(job, job.A, c, c, c, nullptr, job.jblock, floor2,
-                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
-        return false;
-      if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
-        return false;
-      r_new = job.ival[0];
-      // Uc (c x r_new) = A(:, ord) / s, into V.
-      for (int j = me; j < r_new; j += gridDim.x)
-      {
-        const double s = job.sorted[j];
-        const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
-        for (int i = threadIdx.x; i < c; i += blockDim.x)
-          job.V[i + static_cast<int64_t>(j) * c] = s > 0.0 ? a[i] / s : 0.0;
-      }
-      WSYNC();
-      // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
-      if (!wide_gemm(job, r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sm, sh))
-        return false;
-      wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
-      WSYNC();
-    }
-    else if (h >= c)
-    {
-      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-           e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(gridDim.x) * blockDim.x)
-        job.A[e] = X(e % h, e / h);
-      WSYNC();
-      if (job.mixed)
-      {
-        if (!wide_svd_mixed(job, X, h, c, false, floor2, sm, sh, &sweeps, &conv))
-          return false;
-      }
-      else if (!wide_jacobi<double>(job, job.A, h, c, h, nullptr, job.jblock, floor2,
-                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
-        return false;
-      if (!wide_truncate(job, job.A, h, c, h, delta, T, bs, sh))
-        return false;
-      r_new = job.ival[0];
-      for (int j = me; j < r_new; j += gridDim.x)
-      {
-        const double s = job.sorted[j];
-        const double* a = job.A + static_cast<int64_t>(job.ord[j]) * h;
-        for (int i = threadIdx.x; i < h; i += blockDim.x)
-          job.Ub[i + static_cast<int64_t>(j) * h] = s > 0.0 ? a[i] / s : 0.0;
-      }
-      WSYNC();
-      // F = U^T X.
-      if (!wide_gemm(job, r_new, c, h, View{job.Ub, h, 1}, X, job.F, c, 1, sm, sh))
-        return false;
-      WSYNC();
-    }
-    else
-    {
-      // Jacobi on X^T (c x h); V (h x h) accumulates and becomes U.
-      const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-           e < static_cast<int64_t>(c) * h; e += stride)
-        job.A[e] = X(e / c, e % c);
-      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-           e < static_cast<int64_t>(h) * h; e += stride)
-        job.V[e] = (e % h == e / h) ? 1.0 : 0.0;
-      WSYNC();
-      if (job.mixed)
-      {
-        if (!wide_svd_mixed(job, transposed(X), c, h, true, floor2, sm, sh, &sweeps, &conv))
-          return false;
-      }
-      else if (!wide_jacobi<double>(job, job.A, c, h, c, job.V, job.jblock, floor2,
-                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
-        return false;
-      if (!wide_truncate(job, job.A, c, h, c, delta, T, bs, sh))
-        return false;
-      r_new = job.ival[0];
-      for (int j = me; j < r_new; j += gridDim.x)
-      {
-        const int o = job.ord[j];
-        for (int i = threadIdx.x; i < h; i += blockDim.x)
-          job.Ub[i + static_cast<int64_t>(j) * h] = job.V[i + static_cast<int64_t>(o) * h];
-        for (int i = threadIdx.x; i < c; i += blockDim.x)
-          job.F[static_cast<int64_t>(j) * c + i] = job.A[i + static_cast<int64_t>(o) * c];
-      }
-      WSYNC();
-    }
-    if (lead)
-    {
-      if (!conv)
-        set_status(T, kStatusNotConverged);
-      if (sweeps > T.sweeps)
-        T.sweeps = sweeps;
-    }
+    int r_new = 1;
+    if (!wide_left_svd(job, View{cs, c, 1}, h, c, delta, T, bs, sm, sh, &r_new))
+      return false;
     // next (r_new x wn) = F right_unfold(next); core_k <- U (row-major).
     if (!wide_gemm(job, r_new, wn, c, View{job.F, c, 1}, View{ns, wn, 1}, job.Pb, wn, 1, sm, sh))
       return false;
@@ -809,6 +847,126 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
   return true;
 }
 
+// Streaming apply-round (build_streaming_matvec / _matmat,
+// detail/streaming_apply.hpp:39-202, fused cores detail/fused_apply_core.hpp:
+// 33-272) over the whole grid: right-orthogonalise A and X, then per core
+// C = F x A_k x X_k (two contractions and two permutations, never the full
+// product TT) and a truncated SVD of C, F <- diag(s) V^T.  Same steps as
+// stream_tt of the per-TT kernel.
+__device__ bool wide_stream_tt(const WideJob& job, int item, WideSmem sm, CtaShared& sh)
+{
+  double* ar = job.arena;
+  TTInfo& TA = job.tts[job.a_idx[item]];
+  TTInfo& TX = job.tts[job.b_idx[item]];
+  TTInfo& TO = job.tts[job.out_idx[item]];
+  CoreSlot* SA = job.slots + TA.first;
+  CoreSlot* SX = job.slots + TX.first;
+  CoreSlot* SO = job.slots + TO.first;
+  const int d = TA.d;
+  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  if (!wide_right_orth(job, SA, d, sm, sh) || !wide_right_orth(job, SX, d, sm, sh))
+    return false;
+  const double nA = core_norm(ar + SA[0].off, core_size(SA[0]), sh);
+  const double nX = core_norm(ar + SX[0].off, core_size(SX[0]), sh);
+  double delta = 0.0;
+  const int st = wide_norm_step(job, TO, SO, d, nA * nX, sh, &delta);
+  if (st != 0)
+    return st > 0;
+  if (lead)
+    job.Fs[0] = 1.0;
+  WSYNC();
+  int alpha = 1;
+  for (int k = 0; k < d; ++k)
+  {
+    const int a = SA[k].r, b = SA[k].rp;
+    const int m = SA[k].m;
+    const int p = SA[k].n / m;
+    const int sx = SX[k].r, bx = SX[k].rp;
+    const int nout = SX[k].n / p;
+    const int64_t mpb = static_cast<int64_t>(m) * p * b;
+    // Fp (alpha*sx x a): Fp[(al*sx + ax), aa] = F[al, aa*sx + ax].
+    double* Fp = job.S1;
+    WIDE_FOR(t, static_cast<int64_t>(alpha) * sx * a)
+    {
+      const int aa = static_cast<int>(t % a);
+      const int64_t row = t / a;
+      const int al = static_cast<int>(row / sx), ax = static_cast<int>(row % sx);
+      Fp[t] = job.Fs[static_cast<int64_t>(al) * a * sx + static_cast<int64_t>(aa) * sx + ax];
+    }
+    WSYNC();
+    // G1 (alpha*sx x m*p*b) = Fp A_k.
+    double* G1 = job.S2;
+    if (!wide_gemm(job, alpha * sx, static_cast<int>(mpb), a, View{Fp, a, 1},
+                   View{ar + SA[k].off, mpb, 1}, G1, mpb, 1, sm, sh))
+      return false;
+    WSYNC();
+    // G1p ((al, i, bb) x (ax, q)).
+    const int64_t g1p_rows = static_cast<int64_t>(alpha) * m * b;
+    const int64_t g1p_cols = static_cast<int64_t>(sx) * p;
+    double* G1p = job.S1;
+    WIDE_FOR(t, g1p_rows * g1p_cols)
+    {
+      const int64_t row = t / g1p_cols, col = t % g1p_cols;
+      const int bb = static_cast<int>(row % b);
+      const int i = static_cast<int>((row / b) % m);
+      const int al = static_cast<int>(row / (static_cast<int64_t>(b) * m));
+      const int ax = static_cast<int>(col / p), q = static_cast<int>(col % p);
+      G1p[t] = G1[(static_cast<int64_t>(al) * sx + ax) * mpb +
+                  (static_cast<int64_t>(i) * p + q) * b + bb];
+    }
+    WSYNC();
+    // C2 ((al,i,bb) x (j,bx')) = G1p X_k.
+    const int64_t c2_cols = static_cast<int64_t>(nout) * bx;
+    double* C2 = job.S2;
+    if (!wide_gemm(job, static_cast<int>(g1p_rows), static_cast<int>(c2_cols),
+                   static_cast<int>(g1p_cols), View{G1p, g1p_cols, 1},
+                   View{ar + SX[k].off, c2_cols, 1}, C2, c2_cols, 1, sm, sh))
+      return false;
+    WSYNC();
+    // Cj (al, i, j, bb, bx') row-major.
+    double* Cj = C2;
+    if (nout > 1)
+    {
+      Cj = job.S1;
+      WIDE_FOR(t, g1p_rows * c2_cols)
+      {
+        const int bxx = static_cast<int>(t % bx);
+        const int bb = static_cast<int>((t / bx) % b);
+        const int j = static_cast<int>((t / (static_cast<int64_t>(bx) * b)) % nout);
+        const int64_t ai = t / (static_cast<int64_t>(bx) * b * nout);  // al*m + i
+        Cj[t] = C2[(ai * b + bb) * c2_cols + static_cast<int64_t>(j) * bx + bxx];
+      }
+      WSYNC();
+    }
+    const int hrows = alpha * m * nout;
+    const int ccols = b * bx;
+    double* os = ar + SO[k].off;
+    if (k == d - 1)
+    {
+      wide_copy(os, Cj, static_cast<int64_t>(hrows) * ccols);
+      if (lead)
+        set_ranks(SO[k], alpha, ccols);
+      WSYNC();
+      break;
+    }
+    int r_new = 1;
+    if (!wide_left_svd(job, View{Cj, ccols, 1}, hrows, ccols, delta, TO, nullptr, sm, sh, &r_new))
+      return false;
+    // core_k <- U (row-major hrows x r_new); F <- diag(s) V^T.
+    WIDE_FOR(e, static_cast<int64_t>(hrows) * r_new)
+    {
+      const int64_t i = e / r_new, j = e % r_new;
+      os[e] = job.Ub[i + j * hrows];
+    }
+    wide_copy(job.Fs, job.F, static_cast<int64_t>(r_new) * ccols);
+    if (lead)
+      set_ranks(SO[k], alpha, r_new);
+    WSYNC();
+    alpha = r_new;
+  }
+  return true;
+}
+
 __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
 {
   extern __shared__ double dyn_smem[];
@@ -829,9 +987,14 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
     oz.tmem = tmem_base;
   }
   const WideSmem sm{dyn_smem, job.smem_doubles, job.tc ? &oz : nullptr};
+  const bool stream = job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat;
   for (int i = 0; i < job.ntt; ++i)
-    if (!wide_round_tt(job, job.order ? job.order[i] : i, sm, sh))
+  {
+    const bool ok = stream ? wide_stream_tt(job, job.order ? job.order[i] : i, sm, sh)
+                           : wide_round_tt(job, job.order ? job.order[i] : i, sm, sh);
+    if (!ok)
       break;
+  }
   if (job.tc)
   {
     tc::fence_before_sync();

@@ -182,3 +182,27 @@ def test_autotune_keeps_parity(ttg):
         plan.close()
         for y, t in zip(ys, ts):
             _close(y, O.round(t, 1e-8), TOL if prec == ttg.precision.fp64 else MIXED_TOL)
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL), ("mixed", MIXED_TOL)])
+def test_whole_gpu_streaming_matvec_round(ttg, prec, tol):
+    # build_streaming_matvec over the grid (detail/streaming_apply.hpp:39-110)
+    A = O.random_matrix([4] * 6, [4] * 6, 8, 44, fan_in_scale=True)
+    x = O.random([4] * 6, 32, 45, fan_in_scale=True)
+    o = _opts(ttg, 1e-10, ttg.schedule.whole_gpu, precision=ttg.precision[prec],
+              method=ttg.round_method.svd_streaming)
+    y = ttg.matvec_round(A, x, o)
+    _close(y, O.matvec_round(A, x, 1e-10, method="svd_streaming"), tol)
+    y2 = ttg.matvec_round(A, x, _opts(ttg, 1e-10, ttg.schedule.per_tt,
+                                      precision=ttg.precision[prec],
+                                      method=ttg.round_method.svd_streaming))
+    assert O.ranks(y) == O.ranks(y2)
+
+
+def test_whole_gpu_streaming_matmat_round(ttg):
+    # build_streaming_matmat (detail/streaming_apply.hpp:115-202), 4-axis cores
+    A = O.random_matrix([2, 3, 2, 3], [3, 2, 3, 2], 6, 0xCC33)
+    B = O.random_matrix([3, 2, 3, 2], [2, 3, 2, 3], 6, 0xDD44)
+    c = ttg.matmat_round(A, B, _opts(ttg, 1e-10, ttg.schedule.whole_gpu))
+    _close(c, O.matmat_round(A, B, 1e-10))
+    assert c[0].ndim == 4
