@@ -569,10 +569,14 @@ def run_sketch(args):
     ranks = S.sketch_ranks(model, feats, test)
     predict_s = time.perf_counter() - t0
 
-    def timed(opts):
+    tuned = {}
+
+    def timed(opts, tune=False):
         plan = T.Plan("round", test, opts=opts)
         sptr = torch.cuda.current_stream().cuda_stream
         plan.upload(sptr)
+        if tune:  # launch configuration by the autotuner (per TT, or teams of CTAs)
+            tuned[int(opts.precision)] = plan.autotune(sptr)
         for _ in range(args.warmup):
             plan.run(sptr)
         torch.cuda.synchronize()

@@ -79,7 +79,8 @@ typedef enum ttg_precision { TTG_PREC_FP64 = 0, TTG_PREC_MIXED = 1 } ttg_precisi
 typedef enum ttg_schedule {
   TTG_SCHED_AUTO = 0,
   TTG_SCHED_PER_TT = 1,
-  TTG_SCHED_WHOLE_GPU = 2
+  TTG_SCHED_WHOLE_GPU = 2,
+  TTG_SCHED_TEAMS = 3 /* groups of CTAs (>= 4 each), each on its own TT */
 } ttg_schedule;
 
 /* round_options (round/round.hpp:55-105), SVD-relevant fields plus the
@@ -247,8 +248,8 @@ int32_t ttg_plan_run(ttg_plan* plan, void* stream);
  * schedule as a contender; on the mixed path also with and without the
  * sliced-BF16 tensor-core contractions) and keeps the fastest.  *choice
  * (optional): 1-4 = per TT with that many CTAs per SM, 100 + b = whole
- * GPU with block width b (+1000 with tensor-core contractions), 0 = nothing
- * to tune.  Synchronises `stream`; drops a captured
+ * GPU with block width b (+1000 with tensor-core contractions), 10000 + t =
+ * t teams of CTAs, 0 = nothing to tune.  Synchronises `stream`; drops a captured
  * graph (capture again afterwards). */
 int32_t ttg_plan_autotune(ttg_plan* plan, void* stream, int32_t* choice);
 /* enable != 0: capture one run (deep copy from the pristine inputs, the
@@ -263,8 +264,8 @@ int32_t ttg_plan_download(ttg_plan* plan, void* stream, ttg_tensor* outs, double
 /* Device time (ms) of the sweep kernel of the last run(), from events
  * recorded on the run's stream around that launch alone. */
 int32_t ttg_plan_kernel_ms(ttg_plan* plan, float* ms);
-/* Schedule the plan's sweep runs on: TTG_SCHED_PER_TT or
- * TTG_SCHED_WHOLE_GPU (0 for plans without a rounding sweep). */
+/* Schedule the plan's sweep runs on: TTG_SCHED_PER_TT, TTG_SCHED_WHOLE_GPU
+ * or TTG_SCHED_TEAMS (0 for plans without a rounding sweep). */
 int32_t ttg_plan_schedule(const ttg_plan* plan);
 /* Bytes moved host->device by upload and device->host by download. */
 int32_t ttg_plan_io_bytes(const ttg_plan* plan, int64_t* h2d, int64_t* d2h);

@@ -59,6 +59,7 @@ class schedule(enum.IntEnum):
     auto = 0
     per_tt = 1
     whole_gpu = 2
+    teams = 3
 
 
 class TTGError(RuntimeError):
@@ -433,6 +434,8 @@ class Plan:
         v = c.value
         if v in (1, 2, 3, 4):
             return f"per_tt x{v}"
+        if v > 10000:
+            return f"teams x{v - 10000}"
         if v > 1000:
             return f"whole_gpu b={v - 1100} tensor_cores"
         if v > 100:
@@ -467,7 +470,7 @@ class Plan:
     def schedule(self) -> str:
         """'per_tt' or 'whole_gpu' (the device schedule of the sweep), '' if none."""
         v = lib().ttg_plan_schedule(self.h)
-        return {1: "per_tt", 2: "whole_gpu"}.get(v, "")
+        return {1: "per_tt", 2: "whole_gpu", 3: "teams"}.get(v, "")
 
     def io_bytes(self):
         a, b = C.c_int64(), C.c_int64()

@@ -278,6 +278,8 @@ struct ttg_plan
   // whole-GPU schedule (wide_round_kernel)
   bool wide = false;
   int wide_grid = 0;
+  int wide_teams = 1;      // teams of the whole-GPU kernel (1 = all CTAs on one TT)
+  int wide_teams_max = 1;  // teams the work buffers were allocated for
   WideJob wjob{};
   DevMem wdev;
   // byte layout of the device buffer
@@ -462,11 +464,18 @@ int32_t setup_wide(ttg_plan& P)
     }
     cols_max = std::max(cols_max, cols);
   }
-  const bool want = P.opts.schedule == TTG_SCHED_WHOLE_GPU ||
-                    (P.order.size() <= 4 && c_max >= 64);
+  const int64_t items = static_cast<int64_t>(P.order.size());
+  const bool force_whole = P.opts.schedule == TTG_SCHED_WHOLE_GPU;
+  const bool force_teams = P.opts.schedule == TTG_SCHED_TEAMS;
+  const bool big = c_max >= 64;
+  // Whole grid on one TT at a time: forced, or AUTO for a few large TTs.
+  // Teams: forced, or offered to the autotuner for 5..256 large TTs (the
+  // default stays one CTA per TT).
+  const bool want_whole = force_whole || (!force_teams && items <= 4 && big);
+  const bool offer_teams = force_teams || (!force_whole && items > 4 && items <= 256 && big);
   if (stream)
     core_max = std::max(core_max, s_max);
-  if (!want)
+  if (!want_whole && !offer_teams)
     return TTG_OK;
   // Jacobi block pairs: (2 c_max rows + c_max V rows) x 2b columns + 2b norms.
   int jb = 4;
@@ -481,6 +490,11 @@ int32_t setup_wide(ttg_plan& P)
     return fail(TTG_ERR_CUDA, std::string("whole-GPU round setup: ") + cudaGetErrorString(e));
   if (grid < 2)
     return TTG_OK;
+  // Team counts: up to one team per item, at least 4 CTAs per team, 32 teams.
+  int teams_max = 1;
+  if (offer_teams)
+    teams_max = static_cast<int>(std::max<int64_t>(
+      1, std::min<int64_t>({items, static_cast<int64_t>(grid / 4), 32})));
   const int ms = P.opts.max_sweeps > 0 ? P.opts.max_sweeps : 40;
   size_t o = 0;
   auto take = [&](size_t bytes) {
@@ -495,10 +509,14 @@ int32_t setup_wide(ttg_plan& P)
                opart = take(8 * static_cast<size_t>(grid) + 8), oumax = take(8),
                otau = take(8 * c_max), osig = take(8 * c_max),
                osorted = take(8 * c_max), oord = take(4 * c_max), ocn = take(8 * (cols_max + 1)),
-               oival = take(64), orot = take(4 * ms), orel = take(4 * ms), obar = take(sizeof(GridBar)),
+               oival = take(64), orot = take(4 * ms), orel = take(4 * ms),
                oS1 = take(stream ? 8 * static_cast<size_t>(s_max) : 8),
                oS2 = take(stream ? 8 * static_cast<size_t>(s_max) : 8),
                oFs = take(stream ? 8 * static_cast<size_t>(f_max) : 8);
+  // One such block per team, then the teams' barrier words.
+  const size_t team_bytes = o;
+  const size_t obar = team_bytes * static_cast<size_t>(teams_max);
+  o = align256(obar + sizeof(GridBar) * static_cast<size_t>(teams_max));
   TTG_CUDA(P.wdev.ensure(o));
   char* b = static_cast<char*>(P.wdev.p);
   char* d = static_cast<char*>(P.dev.p);
@@ -550,8 +568,21 @@ int32_t setup_wide(ttg_plan& P)
   j.S2 = reinterpret_cast<double*>(b + oS2);
   j.Fs = reinterpret_cast<double*>(b + oFs);
   j.bond_stats = P.opts.bond_stats ? reinterpret_cast<BondStat*>(d + P.off_stats) : nullptr;
-  P.wide = true;
+  j.team_bytes = static_cast<int64_t>(team_bytes);
   P.wide_grid = grid;
+  P.wide_teams_max = teams_max;
+  if (want_whole)
+  {
+    P.wide = true;
+    P.wide_teams = 1;
+  }
+  else if (force_teams)
+  {
+    P.wide = true;
+    P.wide_teams = teams_max;
+  }
+  else
+    P.wide_teams = teams_max;  // offered to the autotuner; per-TT stays the default
   return TTG_OK;
 }
 
@@ -683,6 +714,8 @@ int32_t check_opts(const ttg_round_options* o, const char* op)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown gauge");
   if (o->precision != TTG_PREC_FP64 && o->precision != TTG_PREC_MIXED)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown precision");
+  if (o->schedule < TTG_SCHED_AUTO || o->schedule > TTG_SCHED_TEAMS)
+    return fail(TTG_ERR_ARG, std::string(op) + ": unknown schedule");
   if (o->method == TTG_METHOD_ALS || o->method == TTG_METHOD_DMRG)
     return fail(TTG_ERR_METHOD, std::string(op) + ": als/dmrg rounding is not served here");
   if (o->method < 0 || o->method > TTG_METHOD_SKETCH)
@@ -818,8 +851,11 @@ int32_t plan_run(ttg_plan& P, cudaStream_t st)
     TTG_CUDA(record_event(P.evk0, st));
     if (P.wide)
     {
-      TTG_CUDA(cudaMemsetAsync(P.wjob.bar, 0, sizeof(GridBar), st));
-      TTG_CUDA(launch_wide_round(P.wjob, P.wide_grid, st));
+      TTG_CUDA(cudaMemsetAsync(P.wjob.bar, 0, sizeof(GridBar) * P.wide_teams, st));
+      WideJob j = P.wjob;
+      j.teams = P.wide_teams;
+      const int tsize = P.wide_grid / P.wide_teams;
+      TTG_CUDA(launch_wide_round(j, tsize * P.wide_teams, st));
     }
     else
       launch_round(make_job(P), P.grid, P.cps, st);
@@ -840,12 +876,15 @@ int32_t plan_download_raw(ttg_plan& P, cudaStream_t st)
     TTG_CUDA(cudaMemcpyAsync(P.stats_host.data(), static_cast<char*>(P.dev.p) + P.off_stats,
                              sizeof(BondStat) * P.slots.size(), cudaMemcpyDeviceToHost, st));
   }
-  GridBar bar{};
+  std::vector<GridBar> bars(static_cast<size_t>(std::max(P.wide_teams, 1)));
   if (P.wide)
-    TTG_CUDA(cudaMemcpyAsync(&bar, P.wjob.bar, sizeof(GridBar), cudaMemcpyDeviceToHost, st));
+    TTG_CUDA(cudaMemcpyAsync(bars.data(), P.wjob.bar, sizeof(GridBar) * bars.size(),
+                             cudaMemcpyDeviceToHost, st));
   TTG_CUDA(cudaStreamSynchronize(st));
-  if (P.wide && bar.err)
-    return fail(TTG_ERR_TIMEOUT, "whole-GPU round: a grid barrier wait timed out");
+  if (P.wide)
+    for (const GridBar& bar : bars)
+      if (bar.err)
+        return fail(TTG_ERR_TIMEOUT, "whole-GPU round: a grid barrier wait timed out");
   if (P.opts.bond_stats && !P.slots.empty())
   {
     // 4 doubles per bond, TT by TT.
@@ -1125,7 +1164,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   {
     int code;  // 1/2: per TT, CTAs per SM; 100 + b (+ 1000 with tensor cores): whole GPU
     bool wide;
-    int grid, smem, jblock, tc, cps;
+    int grid, smem, jblock, tc, cps, teams = 1;
   };
   std::vector<Cand> cands;
   const int g1 = std::max(1, std::min(items, sms)), g2 = std::max(1, std::min(items, 2 * sms));
@@ -1138,6 +1177,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   if (g4 > g3 && g4 <= P->scratch_ctas)
     cands.push_back({4, false, g4, kSmemFourPerSm, P->wjob.jblock, P->wjob.tc, 4});
   const bool can_wide = P->wide_grid > 0 && P->wjob.W != nullptr;
+  const int teams0 = P->wide_teams;
   if (can_wide)
   {
     int64_t c_max = 1;
@@ -1147,10 +1187,17 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
         const CoreSlot& c = P->slots[P->tts[t].first + k];
         c_max = std::max<int64_t>(c_max, std::max(c.r, c.rp));
       }
-    for (int tcv = 0; tcv <= P->wjob.mixed; ++tcv)
-      for (int b : {2, 4, 8})
-        if ((6 * c_max + 2) * b <= kSmemOnePerSm)
-          cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv, 1});
+    if (P->wide_teams_max <= 1)
+    {
+      for (int tcv = 0; tcv <= P->wjob.mixed; ++tcv)
+        for (int b : {2, 4, 8})
+          if ((6 * c_max + 2) * b <= kSmemOnePerSm)
+            cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv, 1, 1});
+    }
+    else
+      for (int t : {4, 8, 16, 32})
+        if (t <= P->wide_teams_max)
+          cands.push_back({10000 + t, true, P->wide_grid, kSmemOnePerSm, P->wjob.jblock, 0, 1, t});
   }
   const bool wide0 = P->wide;
   const int grid0 = P->grid, smem0 = P->smem_doubles, jb0 = P->wjob.jblock, tc0 = P->wjob.tc,
@@ -1166,6 +1213,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->wjob.jblock = c.jblock;
     P->wjob.tc = c.tc;
     P->cps = c.cps;
+    P->wide_teams = c.teams;
     float ms = 0.0f;
     for (int rep = 0; rep < 2; ++rep)  // warm, then timed
     {
@@ -1178,10 +1226,12 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     }
     if (P->wide)
     {
-      GridBar bar{};
-      TTG_CUDA(cudaMemcpy(&bar, P->wjob.bar, sizeof(GridBar), cudaMemcpyDeviceToHost));
-      if (bar.err)
-        return fail(TTG_ERR_TIMEOUT, "autotune: a grid barrier wait timed out");
+      std::vector<GridBar> bars(static_cast<size_t>(P->wide_teams));
+      TTG_CUDA(cudaMemcpy(bars.data(), P->wjob.bar, sizeof(GridBar) * bars.size(),
+                          cudaMemcpyDeviceToHost));
+      for (const GridBar& bar : bars)
+        if (bar.err)
+          return fail(TTG_ERR_TIMEOUT, "autotune: a grid barrier wait timed out");
     }
     if (bi < 0 || ms < best)
     {
@@ -1197,6 +1247,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
     P->wjob.jblock = jb0;
     P->wjob.tc = tc0;
     P->cps = cps0;
+    P->wide_teams = teams0;
     return TTG_OK;
   }
   const Cand& c = cands[static_cast<size_t>(bi)];
@@ -1206,6 +1257,7 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
   P->wjob.jblock = c.jblock;
   P->wjob.tc = c.tc;
   P->cps = c.cps;
+  P->wide_teams = c.teams;
   if (choice)
     *choice = c.code;
   return TTG_OK;
@@ -1266,7 +1318,9 @@ int32_t ttg_plan_schedule(const ttg_plan* P)
 {
   if (!P || P->order.empty() || P->job_kind < 0)
     return 0;
-  return P->wide ? TTG_SCHED_WHOLE_GPU : TTG_SCHED_PER_TT;
+  if (!P->wide)
+    return TTG_SCHED_PER_TT;
+  return P->wide_teams > 1 ? TTG_SCHED_TEAMS : TTG_SCHED_WHOLE_GPU;
 }
 
 int32_t ttg_plan_io_bytes(const ttg_plan* P, int64_t* h2d, int64_t* d2h)

@@ -130,6 +130,9 @@ struct WideJob
   int max_rank;
   int max_sweeps;
   int jblock;          // Jacobi block width (columns)
+  int teams;           // groups of CTAs, each rounding its own TTs (1 = whole grid)
+  int rank, size;      // this CTA's rank in its team and the team size (set on the device)
+  int64_t team_bytes;  // stride between the teams' work-buffer blocks
   int mixed;           // 1: FP32 + df64 SVD sweeps
   int tc;              // 1: contractions with K <= 512 on the tensor cores (sliced BF16)
   int kind;            // kJobRound or kJobStreamMatvec / kJobStreamMatmat
@@ -160,7 +163,7 @@ struct WideJob
   unsigned long long* umax;  // grid-wide max of |x| bit patterns
   unsigned int* sweep_rot;  // max_sweeps
   unsigned int* sweep_rel;  // max_sweeps
-  GridBar* bar;
+  GridBar* bar;        // one barrier word per team
   BondStat* bond_stats;
 };
 

@@ -1,4 +1,4 @@
-// Whole-GPU rounding of a few large TTs.
+// Whole-GPU rounding of a few large TTs (or of many, by teams of CTAs).
 //
 // One cooperative launch, one CTA per SM; the CTAs work on one TT at a time
 // and meet at a grid barrier between dependent phases.  Same algorithm and
@@ -42,9 +42,10 @@ namespace ttg
 
 constexpr long long kGridWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
 
-// Bounded grid barrier (sense by generation counter).  All CTAs are
-// co-resident (cooperative launch).  Returns false once any CTA timed out.
-__device__ bool grid_sync(GridBar* gb)
+// Bounded barrier of the `count` CTAs of a team (the whole grid, or a group
+// of it), by generation counter.  All CTAs are co-resident (cooperative
+// launch).  Returns false once any CTA of the team timed out.
+__device__ bool grid_sync(GridBar* gb, unsigned int count)
 {
   __shared__ int ok_sh;
   __syncthreads();
@@ -55,7 +56,7 @@ __device__ bool grid_sync(GridBar* gb)
     volatile int* errp = &gb->err;
     const unsigned int g = *genp;
     __threadfence();
-    if (atomicAdd(&gb->count, 1u) == gridDim.x - 1)
+    if (atomicAdd(&gb->count, 1u) == count - 1)
     {
       atomicExch(&gb->count, 0u);
       __threadfence();
@@ -88,7 +89,7 @@ __device__ bool grid_sync(GridBar* gb)
 #define WSYNC()                 \
   do                            \
   {                             \
-    if (!grid_sync(job.bar))    \
+    if (!grid_sync(job.bar, job.size)) \
       return false;             \
   } while (0)
 
@@ -100,10 +101,10 @@ struct WideSmem
 };
 
 // dst[0..n) = src[0..n), spread over the grid.
-__device__ void wide_copy(double* dst, const double* src, int64_t n)
+__device__ void wide_copy(const WideJob& job, double* dst, const double* src, int64_t n)
 {
-  const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-  for (int64_t t = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n; t += stride)
+  const int64_t stride = static_cast<int64_t>(job.size) * blockDim.x;
+  for (int64_t t = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x; t < n; t += stride)
     dst[t] = src[t];
 }
 
@@ -118,7 +119,7 @@ __device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View 
   {
     const int tm = (M + kOzM - 1) / kOzM, tn = (N + kOzN - 1) / kOzN;
     bool ok = true;
-    for (int t = blockIdx.x; t < tm * tn && ok; t += gridDim.x)
+    for (int t = job.rank; t < tm * tn && ok; t += job.size)
       ok = oz_tile((t / tn) * kOzM, (t % tn) * kOzN, M, N, K, A, B, C, c_rs, c_cs,
                    reinterpret_cast<uint8_t*>(sm.p), *sm.oz, sh);
     if (!ok && threadIdx.x == 0)
@@ -126,7 +127,7 @@ __device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View 
     return ok;
   }
   const int tm = (M + 63) / 64, tn = (N + 63) / 64;
-  for (int t = blockIdx.x; t < tm * tn; t += gridDim.x)
+  for (int t = job.rank; t < tm * tn; t += job.size)
     cta_gemm_tile((t / tn) * 64, (t % tn) * 64, M, N, K, A, B, C, c_rs, c_cs, sh);
   __syncthreads();
   return true;
@@ -138,7 +139,7 @@ __device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View 
 __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, CtaShared& sh,
                        bool* ok)
 {
-  const int P = gridDim.x, me = blockIdx.x;
+  const int P = job.size, me = job.rank;
   const int k = h < c ? h : c;
   const int nown = (c - me + P - 1) / P > 0 ? (c - me + P - 1) / P : 0;
   const bool in_smem = static_cast<int64_t>(nown) * h <= sm.cap;
@@ -206,7 +207,7 @@ __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, Ct
     reflect(0);
   for (int j = 0; j < k; ++j)
   {
-    if (!grid_sync(job.bar))
+    if (!grid_sync(job.bar, job.size))
     {
       *ok = false;
       return k;
@@ -236,7 +237,7 @@ __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, Ct
     for (int i = threadIdx.x; i < k; i += blockDim.x)
       job.R[i + static_cast<int64_t>(l) * k] = (i <= l) ? y[i] : 0.0;
   }
-  if (!grid_sync(job.bar))
+  if (!grid_sync(job.bar, job.size))
     *ok = false;
   return k;
 }
@@ -248,7 +249,7 @@ __device__ void wide_apply_q(const WideJob& job, int h, int kref, const double* 
                              int ncols, double* out, int64_t o_rs, int64_t o_cs, bool eye,
                              WideSmem sm, CtaShared& sh)
 {
-  const int P = gridDim.x, me = blockIdx.x;
+  const int P = job.size, me = job.rank;
   for (int l = me; l < ncols; l += P)
   {
     double* y = (h <= sm.cap) ? sm.p : job.Ub + static_cast<int64_t>(l) * h;
@@ -290,7 +291,7 @@ __device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda,
                             int* conv)
 {
   using S = typename JOps<E>::S;
-  const int P = gridDim.x, me = blockIdx.x;
+  const int P = job.size, me = job.rank;
   const int nblk = (q + b - 1) / b;
   const int NB = nblk + (nblk & 1), npairs = NB / 2;
   E* As = reinterpret_cast<E*>(sm.p);
@@ -383,8 +384,8 @@ __device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda,
 
 // Grid-stride loop bounds of this thread.
 #define WIDE_FOR(e, n)                                                                   \
-  for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < (n); \
-       e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+  for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < (n); \
+       e += static_cast<int64_t>(job.size) * blockDim.x)
 
 // The SVD step of the mixed path over the grid, as cta_jacobi_mixed:
 // FP32 block-pair sweeps on an FP32 copy of src (p x q) accumulating V32,
@@ -396,7 +397,7 @@ __device__ bool wide_jacobi(const WideJob& job, E* A, int p, int q, int64_t lda,
 __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool with_v,
                                double floor2, WideSmem sm, CtaShared& sh, int* sweeps, int* conv)
 {
-  const int me = blockIdx.x;
+  const int me = job.rank;
   float* A32 = reinterpret_cast<float*>(job.Pb);
   float* V32 = reinterpret_cast<float*>(job.T1);
   const int64_t pq = static_cast<int64_t>(p) * q, qq = static_cast<int64_t>(q) * q;
@@ -416,7 +417,7 @@ __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool 
     *job.umax = 0ull;
   WSYNC();
   double ss = 0.0;
-  for (int i = 0; i < static_cast<int>(gridDim.x); ++i)
+  for (int i = 0; i < static_cast<int>(job.size); ++i)
     ss += job.part[i];
   const float floor32 = fmaxf(static_cast<float>(floor2), 1e-12f * static_cast<float>(ss / q));
   int sw32 = 0, cv32 = 0;
@@ -445,7 +446,7 @@ __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool 
     WSYNC();
   }
   // The result is in Vd (T2); V takes it.
-  wide_copy(job.V, Vd, qq);
+  wide_copy(job, job.V, Vd, qq);
   WSYNC();
   if (!wide_gemm(job, p, q, q, src, View{job.V, 1, q}, job.A, 1, p, sm, sh))
     return false;
@@ -501,7 +502,7 @@ __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool 
 __device__ bool wide_truncate(const WideJob& job, const double* A, int p, int q, int64_t lda,
                               double delta, TTInfo& T, BondStat* bs, CtaShared& sh)
 {
-  const int P = gridDim.x, me = blockIdx.x;
+  const int P = job.size, me = job.rank;
   for (int j = me; j < q; j += P)
   {
     const double* a = A + static_cast<int64_t>(j) * lda;
@@ -534,7 +535,7 @@ __device__ bool wide_truncate(const WideJob& job, const double* A, int p, int q,
 // geometric mean from all norms in the same order.
 __device__ bool wide_balance(const WideJob& job, double* ar, CoreSlot* S, int d, CtaShared& sh)
 {
-  const int P = gridDim.x, me = blockIdx.x;
+  const int P = job.size, me = job.rank;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   int64_t base = 0;
   for (int k = 0; k < d - 1; ++k)
@@ -615,7 +616,7 @@ __device__ bool wide_right_orth(const WideJob& job, CoreSlot* S, int d, WideSmem
                                 CtaShared& sh)
 {
   double* ar = job.arena;
-  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  const bool lead = (job.rank == 0 && threadIdx.x == 0);
   for (int k = d - 1; k >= 1; --k)
   {
     const int r = S[k].r, n = S[k].n, rp = S[k].rp;
@@ -633,7 +634,7 @@ __device__ bool wide_right_orth(const WideJob& job, CoreSlot* S, int d, WideSmem
     if (!wide_gemm(job, hp, kk, r, View{ps, r, 1}, View{job.R, kk, 1}, job.Pb, kk, 1, sm, sh))
       return false;
     WSYNC();
-    wide_copy(ps, job.Pb, static_cast<int64_t>(hp) * kk);
+    wide_copy(job, ps, job.Pb, static_cast<int64_t>(hp) * kk);
     if (lead)
     {
       set_ranks(S[k], kk, rp);
@@ -651,7 +652,7 @@ __device__ bool wide_right_orth(const WideJob& job, CoreSlot* S, int d, WideSmem
 __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double delta, TTInfo& T,
                               BondStat* bs, WideSmem sm, CtaShared& sh, int* r_new_out)
 {
-  const int me = blockIdx.x;
+  const int me = job.rank;
   const bool lead = (me == 0 && threadIdx.x == 0);
   const int nsv = h < c ? h : c;
   const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
@@ -663,7 +664,7 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
     if (!ok)
       return false;
     // A = R (c x c), then Jacobi.
-    wide_copy(job.A, job.R, static_cast<int64_t>(c) * c);
+    wide_copy(job, job.A, job.R, static_cast<int64_t>(c) * c);
     WSYNC();
     if (job.mixed)
     {
@@ -677,7 +678,7 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
       return false;
     r_new = job.ival[0];
     // Uc (c x r_new) = A(:, ord) / s, into V.
-    for (int j = me; j < r_new; j += gridDim.x)
+    for (int j = me; j < r_new; j += job.size)
     {
       const double s = job.sorted[j];
       const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
@@ -693,8 +694,8 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
   }
   else if (h >= c)
   {
-    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
-         e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(gridDim.x) * blockDim.x)
+    for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+         e < static_cast<int64_t>(h) * c; e += static_cast<int64_t>(job.size) * blockDim.x)
       job.A[e] = X(e % h, e / h);
     WSYNC();
     if (job.mixed)
@@ -708,7 +709,7 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
     if (!wide_truncate(job, job.A, h, c, h, delta, T, bs, sh))
       return false;
     r_new = job.ival[0];
-    for (int j = me; j < r_new; j += gridDim.x)
+    for (int j = me; j < r_new; j += job.size)
     {
       const double s = job.sorted[j];
       const double* a = job.A + static_cast<int64_t>(job.ord[j]) * h;
@@ -724,11 +725,11 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
   else
   {
     // Jacobi on X^T (c x h); V (h x h) accumulates and becomes U.
-    const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    const int64_t stride = static_cast<int64_t>(job.size) * blockDim.x;
+    for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x;
          e < static_cast<int64_t>(c) * h; e += stride)
       job.A[e] = X(e / c, e % c);
-    for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+    for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x;
          e < static_cast<int64_t>(h) * h; e += stride)
       job.V[e] = (e % h == e / h) ? 1.0 : 0.0;
     WSYNC();
@@ -743,7 +744,7 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
     if (!wide_truncate(job, job.A, c, h, c, delta, T, bs, sh))
       return false;
     r_new = job.ival[0];
-    for (int j = me; j < r_new; j += gridDim.x)
+    for (int j = me; j < r_new; j += job.size)
     {
       const int o = job.ord[j];
       for (int i = threadIdx.x; i < h; i += blockDim.x)
@@ -770,20 +771,20 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
 __device__ int wide_norm_step(const WideJob& job, TTInfo& T, CoreSlot* S, int d, double nrm,
                               CtaShared& sh, double* delta)
 {
-  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  const bool lead = (job.rank == 0 && threadIdx.x == 0);
   if (lead)
     T.norm = nrm;
   if (!isfinite(nrm))
   {
-    if (blockIdx.x == 0)
+    if (job.rank == 0)
       set_status(T, kStatusNan);
     return 1;
   }
   if (nrm == 0.0)
   {
-    if (blockIdx.x == 0)
+    if (job.rank == 0)
       zero_tt(job.arena, S, d);
-    return grid_sync(job.bar) ? 1 : -1;
+    return grid_sync(job.bar, job.size) ? 1 : -1;
   }
   *delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
   if (lead)
@@ -798,7 +799,7 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
   const int d = T.d;
   CoreSlot* S = job.slots + T.first;
   double* ar = job.arena;
-  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  const bool lead = (job.rank == 0 && threadIdx.x == 0);
   if (d <= 1)
     return true;
   if (!wide_right_orth(job, S, d, sm, sh))
@@ -824,10 +825,10 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
     if (!wide_gemm(job, r_new, wn, c, View{job.F, c, 1}, View{ns, wn, 1}, job.Pb, wn, 1, sm, sh))
       return false;
     WSYNC();
-    wide_copy(ns, job.Pb, static_cast<int64_t>(r_new) * wn);
+    wide_copy(job, ns, job.Pb, static_cast<int64_t>(r_new) * wn);
     {
-      const int64_t stride = static_cast<int64_t>(gridDim.x) * blockDim.x;
-      for (int64_t e = blockIdx.x * static_cast<int64_t>(blockDim.x) + threadIdx.x;
+      const int64_t stride = static_cast<int64_t>(job.size) * blockDim.x;
+      for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x;
            e < static_cast<int64_t>(h) * r_new; e += stride)
       {
         const int64_t i = e / r_new, j = e % r_new;
@@ -863,7 +864,7 @@ __device__ bool wide_stream_tt(const WideJob& job, int item, WideSmem sm, CtaSha
   CoreSlot* SX = job.slots + TX.first;
   CoreSlot* SO = job.slots + TO.first;
   const int d = TA.d;
-  const bool lead = (blockIdx.x == 0 && threadIdx.x == 0);
+  const bool lead = (job.rank == 0 && threadIdx.x == 0);
   if (!wide_right_orth(job, SA, d, sm, sh) || !wide_right_orth(job, SX, d, sm, sh))
     return false;
   const double nA = core_norm(ar + SA[0].off, core_size(SA[0]), sh);
@@ -943,7 +944,7 @@ __device__ bool wide_stream_tt(const WideJob& job, int item, WideSmem sm, CtaSha
     double* os = ar + SO[k].off;
     if (k == d - 1)
     {
-      wide_copy(os, Cj, static_cast<int64_t>(hrows) * ccols);
+      wide_copy(job, os, Cj, static_cast<int64_t>(hrows) * ccols);
       if (lead)
         set_ranks(SO[k], alpha, ccols);
       WSYNC();
@@ -958,7 +959,7 @@ __device__ bool wide_stream_tt(const WideJob& job, int item, WideSmem sm, CtaSha
       const int64_t i = e / r_new, j = e % r_new;
       os[e] = job.Ub[i + j * hrows];
     }
-    wide_copy(job.Fs, job.F, static_cast<int64_t>(r_new) * ccols);
+    wide_copy(job, job.Fs, job.F, static_cast<int64_t>(r_new) * ccols);
     if (lead)
       set_ranks(SO[k], alpha, r_new);
     WSYNC();
@@ -987,13 +988,55 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
     oz.tmem = tmem_base;
   }
   const WideSmem sm{dyn_smem, job.smem_doubles, job.tc ? &oz : nullptr};
-  const bool stream = job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat;
-  for (int i = 0; i < job.ntt; ++i)
+  // Teams: the grid splits into `teams` groups of equal size; group g owns
+  // its own work buffers (one block of team_bytes each) and barrier word, and
+  // rounds items g, g + teams, ... (the order is longest first).
+  const int teams = job.teams > 0 ? job.teams : 1;
+  const int tsize = static_cast<int>(gridDim.x) / teams;
+  const int team = static_cast<int>(blockIdx.x) / tsize;
+  __shared__ WideJob tj;  // the team's view of the job, read by every thread
+  if (team < teams && threadIdx.x == 0)
   {
-    const bool ok = stream ? wide_stream_tt(job, job.order ? job.order[i] : i, sm, sh)
-                           : wide_round_tt(job, job.order ? job.order[i] : i, sm, sh);
-    if (!ok)
-      break;
+    tj = job;
+    tj.rank = static_cast<int>(blockIdx.x) % tsize;
+    tj.size = tsize;
+    tj.bar = job.bar + team;
+    const int64_t off = static_cast<int64_t>(team) * job.team_bytes;
+    auto sh_ptr = [off](auto* p) { return reinterpret_cast<decltype(p)>(reinterpret_cast<char*>(p) + off); };
+    tj.W = sh_ptr(job.W);
+    tj.Ub = sh_ptr(job.Ub);
+    tj.Pb = sh_ptr(job.Pb);
+    tj.A = sh_ptr(job.A);
+    tj.R = sh_ptr(job.R);
+    tj.V = sh_ptr(job.V);
+    tj.F = sh_ptr(job.F);
+    tj.T1 = sh_ptr(job.T1);
+    tj.T2 = sh_ptr(job.T2);
+    tj.tau = sh_ptr(job.tau);
+    tj.sig = sh_ptr(job.sig);
+    tj.sorted = sh_ptr(job.sorted);
+    tj.ord = sh_ptr(job.ord);
+    tj.cn = sh_ptr(job.cn);
+    tj.ival = sh_ptr(job.ival);
+    tj.part = sh_ptr(job.part);
+    tj.umax = sh_ptr(job.umax);
+    tj.sweep_rot = sh_ptr(job.sweep_rot);
+    tj.sweep_rel = sh_ptr(job.sweep_rel);
+    tj.S1 = sh_ptr(job.S1);
+    tj.S2 = sh_ptr(job.S2);
+    tj.Fs = sh_ptr(job.Fs);
+  }
+  __syncthreads();
+  if (team < teams)
+  {
+    const bool stream = job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat;
+    for (int i = team; i < job.ntt; i += teams)
+    {
+      const bool ok = stream ? wide_stream_tt(tj, job.order ? job.order[i] : i, sm, sh)
+                             : wide_round_tt(tj, job.order ? job.order[i] : i, sm, sh);
+      if (!ok)
+        break;
+    }
   }
   if (job.tc)
   {

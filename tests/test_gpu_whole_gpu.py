@@ -206,3 +206,18 @@ def test_whole_gpu_streaming_matmat_round(ttg):
     c = ttg.matmat_round(A, B, _opts(ttg, 1e-10, ttg.schedule.whole_gpu))
     _close(c, O.matmat_round(A, B, 1e-10))
     assert c[0].ndim == 4
+
+
+@pytest.mark.parametrize("prec,tol", [("fp64", TOL), ("mixed", MIXED_TOL)])
+def test_teams_schedule_batch(ttg, prec, tol):
+    # groups of CTAs, each rounding its own TTs with team barriers
+    ts = [O.random_uneven(4000 + i) for i in range(12)]
+    res = []
+    ys = ttg.round_batch(ts, _opts(ttg, 1e-8, ttg.schedule.teams, precision=ttg.precision[prec]),
+                         res)
+    for y, t, r in zip(ys, ts, res):
+        assert r.status == 0
+        _close(y, O.round(t, 1e-8), tol)
+    plan = ttg.Plan("round", ts, opts=_opts(ttg, 1e-8, ttg.schedule.teams))
+    assert plan.schedule() == "teams"
+    plan.close()
