@@ -407,8 +407,11 @@ def run_single(args):
     line = {"workload": args.workload, "metric": METRIC, "config": {"workload": inp["desc"]},
             "steps": args.steps, "warmup": args.warmup, "precision": args.precision}
 
-    def timed(plan):
+    def timed(plan, tune=False):
         plan.upload(sptr)
+        if tune:  # launch configuration by the autotuner, then CUDA-graph replays
+            plan.tuned = plan.autotune(sptr)
+            plan.graph(True)
         for _ in range(args.warmup):
             plan.run(sptr)
         torch.cuda.synchronize()
@@ -470,13 +473,14 @@ def run_single(args):
                               method=T.round_method[args.method] if matvec else T.round_method.svd)
         plan = (T.Plan("matvec_round", inp["A"], inp["x"], opts=opts) if matvec
                 else T.Plan("round", [inp["tt"]], opts=opts))
-        ms, clocks = timed(plan)
+        ms, clocks = timed(plan, tune=True)
         kms = []
         for _ in range(3):
             plan.run(sptr)
             kms.append(plan.kernel_ms())
         y = plan.download(sptr)[0]
         sched = plan.schedule()
+        tuned = plan.tuned
         plan.close()
         rout = [y[0].shape[0]] + [c.shape[-1] for c in y]
         F = round_flops(modes, rin, rout)
@@ -484,7 +488,7 @@ def run_single(args):
             F += matvec_flops(ra, rx, modes, [c.shape[2] for c in A])
         kernel_ms = statistics.mean(kms)
         return {"y": y, "ranks_out": rout, "ms": ms, "kernel_ms": kernel_ms, "clocks": clocks,
-                "schedule": sched, "flops": F,
+                "schedule": sched, "flops": F, "tuned": tuned,
                 "achieved": F / (kernel_ms / 1e3) / 1e12}
 
     main = measure(args.precision)
@@ -493,7 +497,8 @@ def run_single(args):
     mixed, plain = (main, other) if args.precision == "mixed" else (other, main)
     line.update({"value": 1e3 / main["ms"], "unit": unit, "ms_per_step": main["ms"],
                  "dtype": "f64" if args.precision == "fp64" else "f64 (fp32/df64 sweeps)",
-                 "schedule": main["schedule"], "ranks_out": main["ranks_out"],
+                 "schedule": main["schedule"], "autotune": main["tuned"], "cuda_graph": True,
+                 "ranks_out": main["ranks_out"],
                  "clocks": main["clocks"],
                  "roofline": {"bound": "fp64", "achieved": main["achieved"], "peak": peak,
                               "unit": "TFLOP/s", "frac": main["achieved"] / peak,
@@ -502,7 +507,8 @@ def run_single(args):
                                             "(tensor_train_gb300/flops.py)"},
                  other_prec if other_prec == "mixed" else "plain_fp64":
                      {"value": 1e3 / other["ms"], "ms_per_step": other["ms"],
-                      "kernel_ms": other["kernel_ms"], "schedule": other["schedule"]},
+                      "kernel_ms": other["kernel_ms"], "schedule": other["schedule"],
+                      "autotune": other["tuned"]},
                  "speedup_mixed_vs_plain_fp64": plain["ms"] / mixed["ms"]})
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O
