@@ -54,6 +54,17 @@ def test_rejects_streaming_method_for_round(ttg):
     assert e.value.status == 3
 
 
+def test_rejects_unknown_schedule_and_precision(ttg):
+    # option validation happens before any device work
+    import numpy as np
+    t = [np.ones((1, 2, 1))]
+    for opts in (ttg.RoundOptions(schedule=7), ttg.RoundOptions(precision=5),
+                 ttg.RoundOptions(eps=-1.0)):
+        with pytest.raises(ttg.TTGError) as e:
+            ttg.round(t, opts)
+        assert e.value.status == 1  # TTG_ERR_ARG
+
+
 def test_no_silent_cpu_fallback(ttg):
     """Without a usable device every compute entry point fails with
     TTG_ERR_CUDA instead of computing on the host."""
