@@ -310,12 +310,23 @@ def cpu_baseline(tts, gpu_outs, sample, plain_outs=None):
         if plain_outs is not None:
             ranks_ok &= O.ranks(plain_outs[i]) == O.ranks(yr)
             perrs.append(O.rel_err(plain_outs[i], yr))
+    # Extra line: the same rounding through numpy/LAPACK (one process; the
+    # BLAS/LAPACK library threads as it likes) on the first 32 sampled TTs.
+    from oracle import numpy_round as NR
+    few = [tts[i] for i in idx[:32]]
+    t0 = time.perf_counter()
+    for t in few:
+        NR.round_tt(t, EPS)
+    np_sec = time.perf_counter() - t0
     return {"value": len(idx) / sec, "unit": "roundings/s", "cores": threads, "kind": "port",
             "sample": f"{len(idx)} of the {len(tts)} TTs (every {stride}th), oracle FP64 "
                       f"round on {threads} host threads, {sec:.2f} s",
             "parity_checked": len(errs), "max_rel_err_vs_oracle": max(errs),
             "max_rel_err_plain_fp64_vs_oracle": max(perrs) if perrs else None,
-            "ranks_equal": bool(ranks_ok)}
+            "ranks_equal": bool(ranks_ok),
+            "numpy_lapack": {"value": len(few) / np_sec, "unit": "roundings/s",
+                             "sample": f"{len(few)} of the sampled TTs, numpy.linalg QR/SVD, "
+                                       "one process"}}
 
 
 def run_reference(args):
