@@ -452,13 +452,29 @@ def run_single(args):
             plan.run(sptr)
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        launches0 = T.kernel_launches()
         with Clocks(0) as clk:
             ev0.record(stream)
             for _ in range(args.steps):
                 plan.run(sptr)
             ev1.record(stream)
             torch.cuda.synchronize()
+        plan.launches = T.kernel_launches() - launches0
         return ev0.elapsed_time(ev1) / args.steps, clk.summary()
+
+    def e2e(call, nbytes_in, out_bytes):
+        """The public host-buffer call (numpy in, numpy out: pack, H2D,
+        kernels, D2H, unpack inside the timed region), wall clock."""
+        for _ in range(min(args.warmup, 2)):
+            out = call()
+        steps = max(1, min(args.steps, 5))
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(steps):
+            out = call()
+        sec = (time.perf_counter() - t0) / steps
+        return {"value": 1.0 / sec, "ms_per_step": sec * 1e3, "h2d_bytes_per_step": nbytes_in,
+                "d2h_bytes_per_step": out_bytes(out)}
 
     if args.workload == "eval_d32":
         idx_pinned = torch.from_numpy(inp["idx"]).pin_memory()
@@ -470,8 +486,12 @@ def run_single(args):
         F = eval_flops(ranks, M)
         nbytes = 4 * inp["idx"].size + 8 * M + 8 * sum(c.size for c in inp["tt"])
         peak = max(T.device_fp64_peak() for _ in range(3))
+        ee = e2e(lambda: T.eval_batch(inp["tt"], inp["idx"]),
+                 4 * inp["idx"].size + 8 * sum(c.size for c in inp["tt"]), lambda o: o.nbytes)
+        ee["value"] *= M
         line.update({"value": M / (ms / 1e3), "unit": "evaluations/s", "ms_per_step": ms,
-                     "dtype": "f64", "clocks": clocks,
+                     "n_gpus": 1, "higher_is_better": True, "dtype": "f64", "clocks": clocks,
+                     "e2e": dict(ee, unit="evaluations/s"), "gpu_launches": plan.launches,
                      "roofline": {"bound": "hbm", "achieved": nbytes / (ms / 1e3) / 1e9,
                                   "peak": measured_peaks()[0], "unit": "GB/s",
                                   "frac": nbytes / (ms / 1e3) / 1e9 / measured_peaks()[0],
@@ -528,16 +548,25 @@ def run_single(args):
         if matvec:
             F += matvec_flops(ra, rx, modes, [c.shape[2] for c in A])
         kernel_ms = statistics.mean(kms)
+        if matvec:
+            call = (lambda: T.matvec_round(inp["A"], inp["x"], opts))
+            nin = 8 * sum(c.size for c in inp["A"] + inp["x"])
+        else:
+            call = (lambda: T.round(inp["tt"], opts))
+            nin = 8 * sum(c.size for c in inp["tt"])
+        ee = e2e(call, nin, lambda o: 8 * sum(c.size for c in o))
         return {"y": y, "ranks_out": rout, "ms": ms, "kernel_ms": kernel_ms, "clocks": clocks,
-                "schedule": sched, "flops": F, "tuned": tuned,
-                "achieved": F / (kernel_ms / 1e3) / 1e12}
+                "schedule": sched, "flops": F, "tuned": tuned, "launches": plan.launches,
+                "achieved": F / (kernel_ms / 1e3) / 1e12, "e2e": ee}
 
     main = measure(args.precision)
     other_prec = "fp64" if args.precision == "mixed" else "mixed"
     other = measure(other_prec)
     mixed, plain = (main, other) if args.precision == "mixed" else (other, main)
     line.update({"value": 1e3 / main["ms"], "unit": unit, "ms_per_step": main["ms"],
+                 "n_gpus": 1, "higher_is_better": True,
                  "dtype": "f64" if args.precision == "fp64" else "f64 (fp32/df64 sweeps)",
+                 "e2e": dict(main["e2e"], unit=unit), "gpu_launches": main["launches"],
                  "schedule": main["schedule"], "autotune": main["tuned"], "cuda_graph": True,
                  "ranks_out": main["ranks_out"],
                  "clocks": main["clocks"],
@@ -547,7 +576,7 @@ def run_single(args):
                  other_prec if other_prec == "mixed" else "plain_fp64":
                      {"value": 1e3 / other["ms"], "ms_per_step": other["ms"],
                       "kernel_ms": other["kernel_ms"], "schedule": other["schedule"],
-                      "autotune": other["tuned"]},
+                      "autotune": other["tuned"], "e2e": dict(other["e2e"], unit=unit)},
                  "speedup_mixed_vs_plain_fp64": plain["ms"] / mixed["ms"]})
     if not args.no_cpu_baseline:
         from oracle import pyoracle as O
