@@ -590,6 +590,33 @@ inline double norm(const tt& a)
   return v;
 }
 
+// frob_norm_apply (algebra/tt_matrix_frob_norm_apply.hpp:36-98): ||A x||_F
+// and ||A B||_F without a host copy of the product.
+inline double frob_norm_apply(const tt_matrix& A, const tt& x)
+{
+  detail::flat fa(A), fx(x);
+  double v = 0.0;
+  detail::check(ttg_frob_norm_apply(&fa.t, &fx.t, &v), "frob_norm_apply");
+  return v;
+}
+inline double frob_norm_apply(const tt_matrix& A, const tt_matrix& B)
+{
+  detail::flat fa(A), fb(B);
+  double v = 0.0;
+  detail::check(ttg_frob_norm_apply(&fa.t, &fb.t, &v), "frob_norm_apply");
+  return v;
+}
+
+// soft_threshold (round/tt_soft_threshold.hpp:42-178): singular values of
+// every bond shrunk by tau; tau <= 0 or d <= 1 returns a copy.
+inline tt soft_threshold(const tt& a, double tau = 0.0)
+{
+  detail::flat fa(a);
+  detail::owned out;
+  detail::check(ttg_soft_threshold(&fa.t, tau, &out.t), "soft_threshold");
+  return detail::to_tt(out.t);
+}
+
 // right_orthogonalize (gauge/tt_orthogonalize.hpp:26-37,
 // gauge/tt_matrix_orthogonalize.hpp:34-86), in place.
 inline void right_orthogonalize(tt& a)

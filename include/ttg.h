@@ -195,6 +195,21 @@ int32_t ttg_eval_batch(const ttg_tensor* a, const int32_t* idx, int32_t M, doubl
 int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out);
 int32_t ttg_norm(const ttg_tensor* a, double* out);
 
+/* Replaces: double frob_norm_apply(const tt_matrix&, const tt&) and
+ *           double frob_norm_apply(const tt_matrix&, const tt_matrix&)
+ *           (algebra/tt_matrix_frob_norm_apply.hpp:36-98): ||A x||_F, or
+ *           ||A B||_F when x is a TT-matrix (cols != NULL). */
+int32_t ttg_frob_norm_apply(const ttg_tensor* A, const ttg_tensor* x, double* out);
+
+/* ---- soft thresholding -------------------------------------------------
+ * Replaces: tt soft_threshold(const tt&, double tau = 0.0)
+ *           (round/tt_soft_threshold.hpp:42-178).  tau <= 0 or d <= 1
+ *           return a copy (no device work); a NaN tau is TTG_ERR_ARG (the
+ *           reference propagates it into the cores).  Singular values beyond
+ *           a bond's current rank (rounding noise of the merged pair) are
+ *           never kept. */
+int32_t ttg_soft_threshold(const ttg_tensor* in, double tau, ttg_tensor* out);
+
 /* ---- host-side input construction (no device work) --------------------
  * Replaces: tt random(const std::vector<int>& shape, int max_rank,
  *           std::uint64_t seed) (factory/tt_factory.hpp:141-207) when

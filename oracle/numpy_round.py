@@ -1,6 +1,7 @@
-"""numpy / LAPACK restatement of detail::round (gauge none) -- TEST
-INFRASTRUCTURE ONLY: a second CPU reference, independent of the C++ oracle's
-own Householder QR and Jacobi SVD, and an extra CPU baseline line.
+"""numpy / LAPACK restatement of detail::round (gauge none) and of
+soft_threshold -- TEST INFRASTRUCTURE ONLY: a second CPU reference,
+independent of the C++ oracle's own Householder QR and Jacobi SVD, and an
+extra CPU baseline line.
 
 Same steps and branches as round/tt_round.hpp:36-134:
   right-to-left QR sweep (detail/orthogonalize.hpp:63-100, r_eff shrink),
@@ -80,4 +81,41 @@ def round_tt(cores, eps=1e-10, max_rank=0):
             col = np.where(norms[k] > 0, geo / np.where(norms[k] > 0, norms[k], 1.0), 1.0)
             c[k] = c[k] * col[None, None, :]
             c[k + 1] = c[k + 1] / col[:, None, None]
+    return c
+
+
+def _right_orthogonalize(c):
+    """right_orthogonalize (gauge/tt_orthogonalize.hpp:26-37) with LAPACK QR."""
+    for k in range(len(c) - 1, 0, -1):
+        r, n, rp = c[k].shape
+        Q, R = np.linalg.qr(c[k].reshape(r, n * rp).T, mode="reduced")
+        kk = Q.shape[1]
+        c[k] = Q.T.reshape(kk, n, rp)
+        rl, nl, _ = c[k - 1].shape
+        c[k - 1] = (c[k - 1].reshape(rl * nl, r) @ R.T).reshape(rl, nl, kk)
+    return c
+
+
+def soft_threshold(cores, tau=0.0):
+    """soft_threshold (round/tt_soft_threshold.hpp:42-178): right-orthogonalise,
+    then right to left per bond: SVD of the merged pair, s <- max(s - tau, 0),
+    keep up to the last positive value; all zero -> rank-1 zero cores."""
+    c = [np.array(x, dtype=np.float64, copy=True) for x in cores]
+    d = len(c)
+    if d <= 1 or tau <= 0.0:
+        return c
+    c = _right_orthogonalize(c)
+    for k in range(d - 1, 0, -1):
+        rl, npr, r = c[k - 1].shape
+        _, nc, rr = c[k].shape
+        M = c[k - 1].reshape(rl * npr, r) @ c[k].reshape(r, nc * rr)
+        U, s, Vt = np.linalg.svd(M, full_matrices=False)
+        pos = np.nonzero(s > tau)[0]
+        if pos.size == 0:
+            c[k - 1] = np.zeros((rl, npr, 1))
+            c[k] = np.zeros((1, nc, rr))
+            continue
+        keep = int(pos[-1]) + 1
+        c[k - 1] = (U[:, :keep] * (s[:keep] - tau)[None, :]).reshape(rl, npr, keep)
+        c[k] = Vt[:keep].reshape(keep, nc, rr)
     return c

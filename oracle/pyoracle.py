@@ -74,6 +74,8 @@ def lib():
         "ttor_inner": (C.c_int, [_P, _P, _DP]),
         "ttor_norm": (C.c_int, [_P, _DP]),
         "ttor_norm_qr": (C.c_double, [_P]),
+        "ttor_frob_norm_apply": (C.c_int, [_P, _P, _DP]),
+        "ttor_soft_threshold": (_P, [_P, C.c_double]),
         "ttor_rel_err": (C.c_double, [_P, _P]),
         "ttor_to_dense": (C.c_longlong, [_P, _DP]),
         "ttor_trace": (None, [C.c_int]),
@@ -280,6 +282,22 @@ def norm(a):
     if lib().ttor_norm(ha.h, C.byref(out)) != 0:
         raise OracleError(lib().ttor_last_error().decode())
     return out.value
+
+
+def frob_norm_apply(A, x):
+    """||A x||_F or ||A B||_F without the product TT
+    (algebra/tt_matrix_frob_norm_apply.hpp:36-98)."""
+    out = C.c_double()
+    hA, hx = H(A), H(x)
+    if lib().ttor_frob_norm_apply(hA.h, hx.h, C.byref(out)) != 0:
+        raise OracleError(lib().ttor_last_error().decode())
+    return out.value
+
+
+def soft_threshold(a, tau=0.0):
+    """Singular-value soft thresholding (round/tt_soft_threshold.hpp:42-178)."""
+    ha = H(a)
+    return Handle(lib().ttor_soft_threshold(ha.h, float(tau))).cores()
 
 
 def norm_qr(a):

@@ -1069,6 +1069,29 @@ inline std::vector<double> eval_batch(const TT& a, const int* idx, int M)
   return out;
 }
 
+// contract_inner_step (detail/contract.hpp:155-205): E (ra x rb) ->
+// E' (rap x rbp) = sum over (a, b, i) of E(a, b) ca(a, i, :) cb(b, i, :).
+inline Mat contract_inner_step(const Mat& E, const Core& ca, const Core& cb)
+{
+  // tmp (rb, n*rap) = E^T (rb x ra) * right_unfold(ca).
+  const int64_t nrap = static_cast<int64_t>(ca.n) * ca.rp;
+  Mat Et = transpose(E);
+  Mat tmp(cb.r, nrap);
+  gemm_nn(cb.r, nrap, ca.r, Et.data(), Et.cols, ca.v.data(), nrap, tmp.data(), nrap);
+  // E' (rap, rbp) = tmp_as^T (rap x rb*n) * left_unfold(cb) (rb*n x rbp).
+  Mat En(ca.rp, cb.rp);
+  const int64_t rbn = static_cast<int64_t>(cb.r) * cb.n;
+  for (int64_t t = 0; t < rbn; ++t)
+    for (int p = 0; p < ca.rp; ++p)
+    {
+      const double x = tmp.v[t * ca.rp + p];
+      const double* brow = &cb.v[t * cb.rp];
+      for (int q = 0; q < cb.rp; ++q)
+        En(p, q) += x * brow[q];
+    }
+  return En;
+}
+
 // inner / norm (algebra/tt_inner.hpp:33-59, detail/contract.hpp:155-205).
 inline double inner(const TT& a, const TT& b)
 {
@@ -1083,27 +1106,7 @@ inline double inner(const TT& a, const TT& b)
   Mat E(1, 1);
   E(0, 0) = 1.0;
   for (int k = 0; k < d; ++k)
-  {
-    const Core& ca = a.c[k];
-    const Core& cb = b.c[k];
-    // tmp (rb, n*rap) = E^T (rb x ra) * right_unfold(ca).
-    const int64_t nrap = static_cast<int64_t>(ca.n) * ca.rp;
-    Mat Et = transpose(E);
-    Mat tmp(cb.r, nrap);
-    gemm_nn(cb.r, nrap, ca.r, Et.data(), Et.cols, ca.v.data(), nrap, tmp.data(), nrap);
-    // E' (rap, rbp) = tmp_as^T (rap x rb*n) * left_unfold(cb) (rb*n x rbp).
-    Mat En(ca.rp, cb.rp);
-    const int64_t rbn = static_cast<int64_t>(cb.r) * cb.n;
-    for (int64_t t = 0; t < rbn; ++t)
-      for (int p = 0; p < ca.rp; ++p)
-      {
-        const double x = tmp.v[t * ca.rp + p];
-        const double* brow = &cb.v[t * cb.rp];
-        for (int q = 0; q < cb.rp; ++q)
-          En(p, q) += x * brow[q];
-      }
-    E = std::move(En);
-  }
+    E = contract_inner_step(E, a.c[k], b.c[k]);
   return E(0, 0);
 }
 
@@ -1111,6 +1114,77 @@ inline double norm(const TT& a)
 {
   const double s = inner(a, a);
   return std::sqrt(std::max(s, 0.0));
+}
+
+// frob_norm_apply (algebra/tt_matrix_frob_norm_apply.hpp:36-98): ||A x||_F
+// or ||A B||_F.  Per site the product core (matvec_core, or matmat_core read
+// as a 3-axis core of mode m*n) goes straight into one contract_inner_step
+// of the product with itself; the product TT is never held whole.
+inline double frob_norm_apply(const TT& A, const TT& X)
+{
+  if (X.matrix)
+    check_matmat(A, X);
+  else
+    check_matvec(A, X);
+  const int d = A.d();
+  if (d == 0)
+    return 0.0;
+  Mat E(1, 1);
+  E(0, 0) = 1.0;
+  for (int k = 0; k < d; ++k)
+  {
+    const Core y = X.matrix ? matmat_core(A.c[k], A.mrow[k], A.ncol[k], X.c[k], X.ncol[k])
+                            : matvec_core(A.c[k], A.mrow[k], A.ncol[k], X.c[k]);
+    E = contract_inner_step(E, y, y);
+  }
+  return std::sqrt(std::max(E(0, 0), 0.0));
+}
+
+// soft_threshold (round/tt_soft_threshold.hpp:42-178): proximal step of the
+// nuclear norm, bond by bond.  d <= 1 or tau <= 0 returns the input.  Else
+// right_orthogonalize, then for k = d-1 .. 1: M = left_unfold(c_{k-1})
+// right_unfold(c_k) (rL*n_{k-1} x n_k*rR), its thin SVD, s' = max(s - tau, 0)
+// and r_keep = the last index with s' > 0; c_{k-1} <- U[:, :r_keep]
+// diag(s'), c_k <- V^T[:r_keep, :].  When every value shrinks to zero both
+// cores become rank-1 zero cores.
+inline TT soft_threshold(TT acc, double tau)
+{
+  const int d = acc.d();
+  if (d <= 1 || tau <= 0.0)
+    return acc;
+  right_orthogonalize(acc);
+  for (int k = d - 1; k >= 1; --k)
+  {
+    Core& prev = acc.c[k - 1];
+    Core& cur = acc.c[k];
+    const int rL = prev.r, np = prev.n, r = prev.rp, nc = cur.n, rR = cur.rp;
+    const int64_t rows = static_cast<int64_t>(rL) * np, cols = static_cast<int64_t>(nc) * rR;
+    Mat M(rows, cols);
+    gemm_nn(rows, cols, r, prev.v.data(), r, cur.v.data(), cols, M.data(), cols);
+    Mat U, Vt;
+    std::vector<double> s;
+    svd_thin(M.data(), rows, cols, U, s, Vt);
+    int keep = 0;
+    for (int j = 0; j < static_cast<int>(s.size()); ++j)
+      if (s[j] > tau)
+        keep = j + 1;
+    if (keep == 0)
+    {
+      prev = Core(rL, np, 1);
+      cur = Core(1, nc, rR);
+      continue;
+    }
+    Core p2(rL, np, keep), c2(keep, nc, rR);
+    for (int64_t i = 0; i < rows; ++i)
+      for (int j = 0; j < keep; ++j)
+        p2.v[static_cast<size_t>(i * keep + j)] = U(i, j) * (s[j] - tau);
+    for (int j = 0; j < keep; ++j)
+      for (int64_t q = 0; q < cols; ++q)
+        c2.v[static_cast<size_t>(j * cols + q)] = Vt(j, q);
+    prev = std::move(p2);
+    cur = std::move(c2);
+  }
+  return acc;
 }
 
 // ---------------------------------------------------------------------------

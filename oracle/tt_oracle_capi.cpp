@@ -241,6 +241,19 @@ int ttor_norm(const ttor_tt* a, double* out)
   }) ? 0 : -1;
 }
 
+int ttor_frob_norm_apply(const ttor_tt* A, const ttor_tt* x, double* out)
+{
+  return guard([&]() -> int {
+    *out = frob_norm_apply(A->t, x->t);
+    return 1;
+  }) ? 0 : -1;
+}
+
+ttor_tt* ttor_soft_threshold(const ttor_tt* a, double tau)
+{
+  return guard([&]() -> ttor_tt* { return new ttor_tt{soft_threshold(a->t, tau)}; });
+}
+
 double ttor_norm_qr(const ttor_tt* a) { return norm_qr(a->t); }
 
 double ttor_rel_err(const ttor_tt* y, const ttor_tt* yref)

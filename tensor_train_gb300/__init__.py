@@ -154,6 +154,8 @@ def lib():
                                        C.POINTER(C.c_double)]),
         "ttg_inner": (C.c_int32, [T, T, C.POINTER(C.c_double)]),
         "ttg_norm": (C.c_int32, [T, C.POINTER(C.c_double)]),
+        "ttg_frob_norm_apply": (C.c_int32, [T, T, C.POINTER(C.c_double)]),
+        "ttg_soft_threshold": (C.c_int32, [T, C.c_double, T]),
         "ttg_plan_create_round": (C.c_int32, [C.c_int32, T, O, C.POINTER(C.c_void_p)]),
         "ttg_plan_create_matvec_round": (C.c_int32, [T, T, O, C.POINTER(C.c_void_p)]),
         "ttg_plan_create_eval": (C.c_int32, [T, C.POINTER(C.c_int32), C.c_int32,
@@ -316,6 +318,15 @@ def right_orthogonalize(a):
     return _take(out)
 
 
+def soft_threshold(a, tau=0.0):
+    """soft_threshold (round/tt_soft_threshold.hpp:42-178): every bond's
+    singular values shrunk to max(s - tau, 0); returns a new TT."""
+    src = _In(a)
+    out = _Tensor()
+    _check(lib().ttg_soft_threshold(C.byref(src.t), float(tau), C.byref(out)), "soft_threshold")
+    return _take(out)
+
+
 def _apply_round(fn, what, A, X, opts, info):
     sa, sx = _In(A), _In(X)
     out, res = _Tensor(), _Result()
@@ -379,6 +390,16 @@ def norm(a) -> float:
     sa = _In(a)
     v = C.c_double()
     _check(lib().ttg_norm(C.byref(sa.t), C.byref(v)), "norm")
+    return v.value
+
+
+def frob_norm_apply(A, x) -> float:
+    """frob_norm_apply (algebra/tt_matrix_frob_norm_apply.hpp:36-98): ||A x||_F,
+    or ||A B||_F when the second operand is a TT-matrix."""
+    sa, sx = _In(A), _In(x)
+    v = C.c_double()
+    _check(lib().ttg_frob_norm_apply(C.byref(sa.t), C.byref(sx.t), C.byref(v)),
+           "frob_norm_apply")
     return v.value
 
 

@@ -356,12 +356,14 @@ int64_t round_need(const Shape& s, int job_kind)
     const int64_t r = s.r[k], n = s.mode(k), rp = s.r[k + 1];
     const int64_t hp = k > 0 ? static_cast<int64_t>(s.r[k - 1]) * s.mode(k - 1) : 0;
     const int64_t wn = k + 1 < d ? static_cast<int64_t>(s.mode(k + 1)) * s.r[k + 2] : 0;
-    if (job_kind == kJobRound || job_kind == kJobRightOrth)
+    if (job_kind == kJobRound || job_kind == kJobRightOrth || job_kind == kJobSoftThreshold)
     {
       if (k >= 1)
         need = std::max(need, need_right_qr(r, n * rp, hp));
       if (k <= d - 2 && job_kind == kJobRound)
         need = std::max(need, need_svd_step(r * n, rp, wn));
+      if (k >= 1 && job_kind == kJobSoftThreshold)
+        need = std::max(need, need_soft_step(hp, n * rp));
     }
     else
     {
@@ -729,8 +731,11 @@ int finish_grid(int64_t items)
   return static_cast<int>(std::max<int64_t>(1, std::min<int64_t>(items, 2LL * sms)));
 }
 
+// job_kind >= 0 replaces the sweep the options select (right_orthogonalize,
+// soft_threshold); it is fixed before the layout, which sizes the scratch
+// and picks the schedule for it.
 int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
-                         const ttg_round_options* opts, const char* op)
+                         const ttg_round_options* opts, const char* op, int job_kind = -1)
 {
   if (int32_t st = check_opts(opts, op))
     return st;
@@ -745,6 +750,8 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
   P.kind = kPlanRound;
   P.job_kind = sketch ? kJobRoundSketch
                       : (opts->gauge == TTG_GAUGE_RIGHT_CANONICAL ? kJobRoundRight : kJobRound);
+  if (job_kind >= 0)
+    P.job_kind = job_kind;
   P.shapes.resize(static_cast<size_t>(count));
   int64_t need = 64;
   std::vector<std::pair<double, int>> cost;
@@ -1453,15 +1460,55 @@ int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   std::lock_guard<std::mutex> lk(g_mu);
   ttg_round_options o{};
   ttg_plan P;
-  if (int32_t st = build_round_plan(P, 1, in, &o, "right_orthogonalize"))
+  if (int32_t st = build_round_plan(P, 1, in, &o, "right_orthogonalize", kJobRightOrth))
     return st;
-  P.job_kind = kJobRightOrth;
   if (P.shapes[0].d <= 1)
     return copy_through(P.shapes[0], out);
   float ms = 0.0f;
   if (int32_t st = execute(P, &ms))
     return st;
   return emit_tensor(P, 0, P.shapes[0].matrix, P.shapes[0].m, P.shapes[0].n, out);
+}
+
+// soft_threshold (round/tt_soft_threshold.hpp:42-178).  d <= 1 or
+// tau <= 0 return a copy of the input, as the reference does; otherwise one
+// CTA sweeps the TT: right_orthogonalize, then the soft step of every bond
+// right to left (job kind kJobSoftThreshold, tau in the job's eps).
+int32_t ttg_soft_threshold(const ttg_tensor* in, double tau, ttg_tensor* out)
+{
+  g_err.clear();
+  if (!in || !out)
+    return fail(TTG_ERR_ARG, "soft_threshold: null argument");
+  if (std::isnan(tau))
+    return fail(TTG_ERR_ARG, "soft_threshold: tau is NaN");
+  Shape s;
+  if (int32_t st = describe(in, "soft_threshold", s))
+    return st;
+  if (s.matrix)
+    return fail(TTG_ERR_ARG, "soft_threshold: takes a tt, not a tt_matrix");
+  if (s.d <= 1 || tau <= 0.0)
+    return copy_through(s, out);
+  for (int k = 1; k < s.d; ++k)
+    if (static_cast<int64_t>(s.r[k - 1]) * s.mode(k - 1) > INT32_MAX ||
+        static_cast<int64_t>(s.mode(k)) * s.r[k + 1] > INT32_MAX)
+      return fail(TTG_ERR_SHAPE, "soft_threshold: dimension product exceeds INT_MAX");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_round_options o{};
+  o.eps = tau;
+  o.precision = TTG_PREC_FP64;
+  o.schedule = TTG_SCHED_PER_TT;
+  ttg_plan P;
+  PoolLease lease(P);
+  if (int32_t st = build_round_plan(P, 1, in, &o, "soft_threshold", kJobSoftThreshold))
+    return st;
+  float ms = 0.0f;
+  if (int32_t st = execute(P, &ms))
+    return st;
+  if (int32_t bad = first_bad_status(P))
+    return fail(bad, std::string("soft_threshold: device status ") + ttg_status_string(bad));
+  return emit_tensor(P, 0, false, s.m, s.n, out);
 }
 
 // ---------------------------------------------------------------------------
@@ -1681,6 +1728,76 @@ int32_t ttg_matvec(const ttg_tensor* A, const ttg_tensor* x, ttg_tensor* out)
 int32_t ttg_matmat(const ttg_tensor* A, const ttg_tensor* B, ttg_tensor* out)
 {
   return apply_round_common(A, B, nullptr, out, nullptr, true, 0, "matmat");
+}
+
+// frob_norm_apply (algebra/tt_matrix_frob_norm_apply.hpp:36-98): the
+// product cores (matvec_core, or matmat_core packed as 3-axis cores of mode
+// m*n) are formed in the arena by the apply kernels, then one CTA runs the
+// contract_inner_step chain of the product with itself.  The product stays
+// on the device (the reference avoids holding it for host-memory reasons;
+// it is sum_k r_k^A r_k^x m_k r_{k+1}^A r_{k+1}^x doubles of HBM here).
+int32_t ttg_frob_norm_apply(const ttg_tensor* a, const ttg_tensor* x, double* out)
+{
+  g_err.clear();
+  const char* op = "frob_norm_apply";
+  if (!out)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null output");
+  Shape A, X;
+  if (int32_t st = describe(a, op, A))
+    return st;
+  if (int32_t st = describe(x, op, X))
+    return st;
+  if (A.d != X.d)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": d mismatch (a.d=" + std::to_string(A.d) +
+                                   ", x.d=" + std::to_string(X.d) + ")");
+  if (A.d == 0)
+  {
+    *out = 0.0;
+    return TTG_OK;
+  }
+  if (int32_t st = check_apply(A, X, X.matrix, op))
+    return st;
+  for (int k = 0; k < A.d; ++k)
+    if (static_cast<int64_t>(A.m[k]) * (X.matrix ? X.n[k] : 1) > INT32_MAX)
+      return fail(TTG_ERR_SHAPE, std::string(op) + ": m*n product exceeds INT_MAX");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_plan P;
+  PoolLease lease(P);
+  if (int32_t st = build_apply_plan(P, A, X, false, nullptr))
+    return st;
+  const TTInfo ty = P.tts[P.out_tts[0]];
+  int64_t env = 1, tmp = 1;
+  for (int k = 0; k < ty.d; ++k)
+  {
+    const CoreSlot& c = P.slots[ty.first + k];
+    env = std::max(env, static_cast<int64_t>(c.r) * c.r);
+    env = std::max(env, static_cast<int64_t>(c.rp) * c.rp);
+    tmp = std::max(tmp, static_cast<int64_t>(c.r) * c.n * c.rp);
+  }
+  env = a32(env);
+  P.scratch_stride = 2 * env + a32(tmp) + 32;
+  if (int32_t st = layout_and_alloc(P))
+    return st;
+  cudaStream_t st = lib_stream();
+  if (int32_t e = plan_upload(P, st))
+    return e;
+  if (int32_t e = plan_run(P, st))
+    return e;
+  char* d = static_cast<char*>(P.dev.p);
+  double* scratch = reinterpret_cast<double*>(d + P.off_scratch);
+  const CoreSlot* S = reinterpret_cast<const CoreSlot*>(d + P.off_slots);
+  launch_inner(reinterpret_cast<double*>(d + P.off_arena), S + ty.first, S + ty.first, ty.d,
+               scratch, env, scratch + P.scratch_stride - 8, st);
+  g_launches += 1;
+  TTG_CUDA(cudaGetLastError());
+  double v = 0.0;
+  TTG_CUDA(cudaMemcpyAsync(&v, scratch + P.scratch_stride - 8, sizeof(double),
+                           cudaMemcpyDeviceToHost, st));
+  TTG_CUDA(cudaStreamSynchronize(st));
+  *out = std::sqrt(std::max(v, 0.0));
+  return TTG_OK;
 }
 
 int32_t ttg_plan_create_matvec_round(const ttg_tensor* a, const ttg_tensor* x,

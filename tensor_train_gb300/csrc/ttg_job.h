@@ -52,6 +52,12 @@ TTG_HD inline int64_t need_svd_step_right(int64_t w, int64_t r, int64_t h_prev)
 {
   return a32(h_prev * r) + need_left_svd(w, r);
 }
+// One bond of soft_threshold: the merged pair M (h = rL*n_prev rows,
+// c = n_cur*rR columns) and its SVD.
+TTG_HD inline int64_t need_soft_step(int64_t h, int64_t c)
+{
+  return a32(h * c) + need_left_svd(h, c);
+}
 // One streaming step: F buffer capacity fcap, F rows alpha, operator core
 // (a, m, p, b), operand core (sx, p*nout, bx).
 TTG_HD inline int64_t need_stream_step(int64_t fcap, int64_t alpha, int64_t a, int64_t m,
@@ -106,6 +112,7 @@ enum JobKind : int32_t
   kJobStreamMatvec = 3,   // build_streaming_matvec (pairs of TTs)
   kJobStreamMatmat = 4,   // build_streaming_matmat
   kJobRoundSketch = 5,    // randomised sketch rounding with an exact check and fallback
+  kJobSoftThreshold = 6,  // right_orthogonalize, then R->L singular-value soft thresholding
 };
 
 // Grid barrier word of the whole-GPU kernel (zeroed before each launch).

@@ -97,9 +97,11 @@ __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* 
 // otherwise decompose X directly -- by columns when h >= c, by rows (the
 // transpose, accumulating V) when h < c.
 
+// s_out (optional) receives the singular values, descending (c or h of them).
 __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
                         bool mixed, Bump bump, Smem sm, double** Ut_out, double** F_out,
-                        TTInfo& T, CtaShared& sh, BondStat* bs = nullptr)
+                        TTInfo& T, CtaShared& sh, BondStat* bs = nullptr,
+                        double** s_out = nullptr)
 {
   double* sig;
   double* sorted;
@@ -223,6 +225,8 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
     __syncthreads();
     *Ut_out = U;
     *F_out = F;
+    if (s_out)
+      *s_out = sorted;
     return r_new;
   }
   if (h >= c)
@@ -284,6 +288,8 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
     __syncthreads();
     *Ut_out = U;
     *F_out = F;
+    if (s_out)
+      *s_out = sorted;
     return r_new;
   }
   // h < c: Jacobi on X^T (c x h), V (h x h) accumulates the rotations and
@@ -351,6 +357,8 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
   __syncthreads();
   *Ut_out = U;
   *F_out = F;
+  if (s_out)
+    *s_out = sorted;
   return r_new;
 }
 
@@ -458,6 +466,61 @@ __device__ __noinline__ void svd_step_right(const RoundJob& job, double* ar, Cor
 
 
 
+
+// One bond of soft_threshold (round/tt_soft_threshold.hpp:64-175): SVD of
+// M = left_unfold(prev) right_unfold(cur) (h x c, FP64), s' = max(s - tau, 0);
+// prev <- U diag(s') over the kept columns, cur <- V^T (the rows of
+// diag(s) V^T that left_svd returns, divided by s).  All values at or below
+// tau: both cores become rank-1 zero cores.  M = L R with an inner dimension
+// of r has at most r nonzero singular values; any further ones are rounding
+// noise (~1e-16 ||M||) and are never kept, so both cores fit their slots.
+__device__ __noinline__ void soft_step(const RoundJob& job, double* ar, CoreSlot& prev,
+                                       CoreSlot& cur, double tau, Bump bump, Smem sm, TTInfo& T,
+                                       CtaShared& sh)
+{
+  const int rL = prev.r, np = prev.n, r = prev.rp, nc = cur.n, rR = cur.rp;
+  const int h = rL * np, c = nc * rR;
+  double* ps = ar + prev.off;
+  double* cs = ar + cur.off;
+  double* M = bump.take(static_cast<int64_t>(h) * c);
+  cta_gemm(h, c, r, View{ps, r, 1}, View{cs, c, 1}, M, c, 1, sh);
+  __syncthreads();
+  double *U, *F, *s;
+  const int rn = left_svd(View{M, c, 1}, h, c, 0.0, 0, job.max_sweeps, false, bump, sm, &U, &F,
+                          T, sh, nullptr, &s);
+  if (threadIdx.x == 0)
+  {
+    int keep = 0;
+    for (int j = 0; j < rn; ++j)
+      if (s[j] > tau)
+        keep = j + 1;
+    sh.ival[1] = keep < r ? keep : r;
+  }
+  __syncthreads();
+  const int keep = sh.ival[1];
+  if (keep == 0)
+  {
+    for (int64_t t = threadIdx.x; t < h; t += blockDim.x)
+      ps[t] = 0.0;
+    for (int64_t t = threadIdx.x; t < c; t += blockDim.x)
+      cs[t] = 0.0;
+    set_ranks(prev, rL, 1);
+    set_ranks(cur, 1, rR);
+    __syncthreads();
+    return;
+  }
+  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * keep; t += blockDim.x)
+  {
+    const int64_t i = t / keep;
+    const int j = static_cast<int>(t % keep);
+    ps[t] = U[i + static_cast<int64_t>(j) * h] * (s[j] - tau);
+  }
+  for (int64_t t = threadIdx.x; t < static_cast<int64_t>(keep) * c; t += blockDim.x)
+    cs[t] = F[t] / s[t / c];
+  set_ranks(prev, rL, keep);
+  set_ranks(cur, keep, rR);
+  __syncthreads();
+}
 
 // Norm balancing (round/tt_round.hpp:65-124).
 __device__ __noinline__ void balance(double* ar, CoreSlot* S, int d, Bump bump, CtaShared& sh)
@@ -572,6 +635,18 @@ __device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scra
     }
     if (job.kind == kJobRightOrth)
       return;
+    if (job.kind == kJobSoftThreshold)
+    {
+      // soft_threshold: eps carries tau.
+      for (int k = d - 1; k >= 1; --k)
+      {
+        if (!fits(job, need_soft_step(static_cast<int64_t>(S[k - 1].r) * S[k - 1].n,
+                                      static_cast<int64_t>(S[k].n) * S[k].rp), T))
+          return;
+        soft_step(job, ar, S[k - 1], S[k], eps, Bump{scratch}, sm, T, sh);
+      }
+      return;
+    }
     const double nrm = core_norm(ar + S[0].off, core_size(S[0]), sh);
     if (threadIdx.x == 0)
       T.norm = nrm;
