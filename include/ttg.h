@@ -162,6 +162,11 @@ int32_t ttg_round_batch(int32_t count, const ttg_tensor* ins, const ttg_round_op
  * and right_orthogonalize(tt_matrix&) (gauge/tt_matrix_orthogonalize.hpp:34-86). */
 int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out);
 
+/* Replaces: void detail::left_orthogonalize(tt&) (gauge/tt_orthogonalize.hpp:39-58),
+ *           the gauge sweep of round_right_canonical and of the Python
+ *           binding's left_orthogonalize (bind_py/tensor_train/__init__.py:662). */
+int32_t ttg_left_orthogonalize(const ttg_tensor* in, ttg_tensor* out);
+
 /* ---- apply + round -----------------------------------------------------
  * Replaces: tt matvec_round(const tt_matrix&, const tt&, const round_options&,
  *           round_result*) (round/matvec_round.hpp:42-91): svd = round(matvec)

@@ -146,6 +146,7 @@ def lib():
         "ttg_round": (C.c_int32, [T, O, T, R]),
         "ttg_round_batch": (C.c_int32, [C.c_int32, T, O, T, R]),
         "ttg_right_orthogonalize": (C.c_int32, [T, T]),
+        "ttg_left_orthogonalize": (C.c_int32, [T, T]),
         "ttg_matvec_round": (C.c_int32, [T, T, O, T, R]),
         "ttg_matmat_round": (C.c_int32, [T, T, O, T, R]),
         "ttg_matvec": (C.c_int32, [T, T, T]),
@@ -315,6 +316,14 @@ def right_orthogonalize(a):
     src = _In(a)
     out = _Tensor()
     _check(lib().ttg_right_orthogonalize(C.byref(src.t), C.byref(out)), "right_orthogonalize")
+    return _take(out)
+
+
+def left_orthogonalize(a):
+    """detail::left_orthogonalize (gauge/tt_orthogonalize.hpp:39-58); returns a new TT."""
+    src = _In(a)
+    out = _Tensor()
+    _check(lib().ttg_left_orthogonalize(C.byref(src.t), C.byref(out)), "left_orthogonalize")
     return _take(out)
 
 

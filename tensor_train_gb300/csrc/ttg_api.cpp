@@ -1470,6 +1470,28 @@ int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   return emit_tensor(P, 0, P.shapes[0].matrix, P.shapes[0].m, P.shapes[0].n, out);
 }
 
+// detail::left_orthogonalize (gauge/tt_orthogonalize.hpp:39-58): the L->R
+// QR sweep, cores 0..d-2 left-orthogonal.
+int32_t ttg_left_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
+{
+  g_err.clear();
+  if (!in || !out)
+    return fail(TTG_ERR_ARG, "left_orthogonalize: null argument");
+  if (int32_t st = need_device())
+    return st;
+  std::lock_guard<std::mutex> lk(g_mu);
+  ttg_round_options o{};
+  ttg_plan P;
+  if (int32_t st = build_round_plan(P, 1, in, &o, "left_orthogonalize", kJobLeftOrth))
+    return st;
+  if (P.shapes[0].d <= 1)
+    return copy_through(P.shapes[0], out);
+  float ms = 0.0f;
+  if (int32_t st = execute(P, &ms))
+    return st;
+  return emit_tensor(P, 0, P.shapes[0].matrix, P.shapes[0].m, P.shapes[0].n, out);
+}
+
 // soft_threshold (round/tt_soft_threshold.hpp:42-178).  d <= 1 or
 // tau <= 0 return a copy of the input, as the reference does; otherwise one
 // CTA sweeps the TT: right_orthogonalize, then the soft step of every bond

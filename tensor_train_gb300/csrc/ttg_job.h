@@ -113,6 +113,7 @@ enum JobKind : int32_t
   kJobStreamMatmat = 4,   // build_streaming_matmat
   kJobRoundSketch = 5,    // randomised sketch rounding with an exact check and fallback
   kJobSoftThreshold = 6,  // right_orthogonalize, then R->L singular-value soft thresholding
+  kJobLeftOrth = 7,       // left_orthogonalize only (the L->R QR sweep)
 };
 
 // Grid barrier word of the whole-GPU kernel (zeroed before each launch).

@@ -623,8 +623,9 @@ __device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scra
   if (d <= 1)
     return;
   // gauge none (detail::round) for plain, sketch-finishing and orthogonalise
-  // jobs; round_right_canonical only for kJobRoundRight.
-  if (job.kind != kJobRoundRight)
+  // jobs; round_right_canonical for kJobRoundRight, whose L->R QR sweep is
+  // also left_orthogonalize (kJobLeftOrth).
+  if (job.kind != kJobRoundRight && job.kind != kJobLeftOrth)
   {
     for (int k = d - 1; k >= 1; --k)
     {
@@ -684,6 +685,8 @@ __device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scra
       return;
     left_qr_step(ar, S[k], S[k + 1], Bump{scratch}, sm, job.mixed != 0, sh);
   }
+  if (job.kind == kJobLeftOrth)
+    return;
   const double nrm = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
   if (threadIdx.x == 0)
     T.norm = nrm;
