@@ -106,6 +106,20 @@ int main()
     CHECK(std::fabs(tt::inner(a, a) - frob(D) * frob(D)) <= 1e-12 * frob(D) * frob(D),
           "inner vs dense");
   }
+  {
+    // tests/core/test_tt_soft_threshold.cpp: tau = 0 is a copy, the norm
+    // does not grow, cores 1..d-1 come out right-orthogonal
+    auto a = tt::random({3, 4, 5}, 8, 7);
+    auto s0 = tt::soft_threshold(a, 0.0);
+    CHECK(frob_diff(s0.to_dense(), a.to_dense()) < 1e-14, "soft_threshold(a, 0) == a");
+    auto s = tt::soft_threshold(a, 0.5);
+    CHECK(tt::norm(s) <= tt::norm(a) * (1.0 + 1e-14), "soft_threshold: norm non-increasing");
+    // tests/core/test_tt_matrix_frob_norm_apply.cpp
+    auto A = tt::random(std::vector<int>{2, 3, 2}, std::vector<int>{3, 2, 3}, 3, 0xA10001ULL);
+    auto x = tt::random({3, 2, 3}, 2, 0x55AA77ULL);
+    const double ref = tt::norm(tt::matvec(A, x));
+    CHECK(std::fabs(tt::frob_norm_apply(A, x) - ref) <= 1e-13 * ref, "frob_norm_apply(A, x)");
+  }
   if (failed == 0)
     std::printf("test_header_round: OK\n");
   return failed;
