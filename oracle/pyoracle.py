@@ -75,6 +75,8 @@ def lib():
         "ttor_norm": (C.c_int, [_P, _DP]),
         "ttor_norm_qr": (C.c_double, [_P]),
         "ttor_frob_norm_apply": (C.c_int, [_P, _P, _DP]),
+        "ttor_apply_core": (C.c_int, [C.c_int, _DP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
+                                      _DP, C.c_int, C.c_int, C.c_int, _DP, _DP]),
         "ttor_soft_threshold": (_P, [_P, C.c_double]),
         "ttor_rel_err": (C.c_double, [_P, _P]),
         "ttor_to_dense": (C.c_longlong, [_P, _DP]),
@@ -292,6 +294,27 @@ def frob_norm_apply(A, x):
     if lib().ttor_frob_norm_apply(hA.h, hx.h, C.byref(out)) != 0:
         raise OracleError(lib().ttor_last_error().decode())
     return out.value
+
+
+def apply_core(A, X, F=None):
+    """One product core: matvec_core / matmat_core (apply/tt_matrix_apply.hpp:40-224)
+    when F is None, else fused_apply_core with the left factor F
+    (detail/fused_apply_core.hpp:33-272).  A is (a, m, p, b); X is (sx, p, bx)
+    or (sx, p, nout, bx).  Returns (alpha, m, bx*b) or (alpha, m, nout, b*bx)."""
+    A = np.ascontiguousarray(A, np.float64)
+    X = np.ascontiguousarray(X, np.float64)
+    a, m, p, b = A.shape
+    sx, bx = X.shape[0], X.shape[-1]
+    nout = X.shape[2] if X.ndim == 4 else 1
+    alpha = a * sx if F is None else F.shape[0]
+    Fa = (np.zeros(1) if F is None else np.ascontiguousarray(F, np.float64))
+    out = np.zeros(alpha * m * nout * b * bx)
+    if lib().ttor_apply_core(0 if F is None else 1, Fa.ctypes.data_as(_DP), alpha, a, m, p, b,
+                             A.ctypes.data_as(_DP), sx, nout, bx, X.ctypes.data_as(_DP),
+                             out.ctypes.data_as(_DP)) != 0:
+        raise OracleError(lib().ttor_last_error().decode())
+    shp = (alpha, m, b * bx) if X.ndim == 3 else (alpha, m, nout, b * bx)
+    return out.reshape(shp)
 
 
 def soft_threshold(a, tau=0.0):

@@ -241,6 +241,32 @@ int ttor_norm(const ttor_tt* a, double* out)
   }) ? 0 : -1;
 }
 
+// Core-level products for the fused-apply known-answer test
+// (tests/core/test_tt_fused_apply_core.cpp): A (a, m, p, b), X (sx, p*nout,
+// bx); fused = 1 forms F (alpha x a*sx) x A x X through fused_apply_core,
+// fused = 0 forms matvec_core (nout = 1) or matmat_core.  out holds
+// alpha*m*nout*b*bx doubles (alpha = a*sx when not fused).
+int ttor_apply_core(int fused, const double* F, int alpha, int a, int m, int p, int b,
+                    const double* A, int sx, int nout, int bx, const double* X, double* out)
+{
+  return guard([&]() -> int {
+    Core Ac(a, m * p, b), Xc(sx, p * nout, bx);
+    std::memcpy(Ac.v.data(), A, sizeof(double) * Ac.size());
+    std::memcpy(Xc.v.data(), X, sizeof(double) * Xc.size());
+    Core y;
+    if (fused)
+    {
+      Mat Fm(alpha, static_cast<int64_t>(a) * sx);
+      std::memcpy(Fm.data(), F, sizeof(double) * Fm.v.size());
+      y = fused_apply_core(Fm, Ac, m, p, Xc, nout);
+    }
+    else
+      y = nout == 1 ? matvec_core(Ac, m, p, Xc) : matmat_core(Ac, m, p, Xc, nout);
+    std::memcpy(out, y.v.data(), sizeof(double) * y.size());
+    return 1;
+  }) ? 0 : -1;
+}
+
 int ttor_frob_norm_apply(const ttor_tt* A, const ttor_tt* x, double* out)
 {
   return guard([&]() -> int {
