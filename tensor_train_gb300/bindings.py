@@ -14,7 +14,7 @@ Rounding, apply, orthogonalisation, soft thresholding, norms, inner products
 and evaluation run on the GPU through the C-ABI; factories, algebra
 (``add``/``axpby``/``scale``) and ``to_dense`` are host work, as in the
 reference.  Constructions outside the rounding path (``from_dense``,
-``from_samples``, ``hadamard``, ``diag_from_tt``, ALS/DMRG rounding) raise
+``from_samples``, ``hadamard``, ALS/DMRG rounding) raise
 ``NotImplementedError`` or the library's method error.
 """
 from __future__ import annotations
@@ -485,7 +485,15 @@ class TensorTrainMatrix:
 
     @staticmethod
     def diag_from_tt(tt):
-        raise NotImplementedError("diag_from_tt is outside the rounding path")
+        """diag(v) as a TT-matrix with v's ranks: core k (r, n, n, r') holds
+        v_k(a, i, b) at (a, i, i, b) (factory/tt_matrix_factory.hpp)."""
+        cores = []
+        for c in _tt_cores(tt):
+            r, n, rp = c.shape
+            m = np.zeros((r, n, n, rp))
+            m[:, np.arange(n), np.arange(n), :] = c
+            cores.append(m)
+        return TensorTrainMatrix(cores)
 
     @staticmethod
     def from_samples(func, row_shape, col_shape, opts=None, **kwargs):
