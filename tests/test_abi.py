@@ -79,3 +79,36 @@ def test_no_silent_cpu_fallback(ttg):
     with pytest.raises(ttg.TTGError) as e:
         ttg.round([np.ones((1, 2, 2)), np.ones((2, 2, 1))], ttg.RoundOptions(eps=1e-8))
     assert e.value.status == 9
+
+
+def test_frob_norm_apply_argument_checks(ttg):
+    # check_matvec_compatible / check_matmat_compatible run before any
+    # device work; d = 0 is ||A x|| = 0 (tt_matrix_frob_norm_apply.hpp:38-41)
+    import numpy as np
+    A = [np.ones((1, 2, 3, 1))]
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.frob_norm_apply(A, [np.ones((1, 2, 1))])      # mode mismatch (3 vs 2)
+    assert e.value.status == 2
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.frob_norm_apply([np.ones((1, 3, 1))], [np.ones((1, 3, 1))])   # A not a TT-matrix
+    assert e.value.status == 1
+    with pytest.raises(ttg.TTGError) as e:
+        ttg.frob_norm_apply(A + A, [np.ones((1, 3, 1))])  # d mismatch
+    assert e.value.status == 2
+    assert ttg.frob_norm_apply([], []) == 0.0
+
+
+def test_no_silent_cpu_fallback_new_entries(ttg):
+    try:
+        import torch
+        if torch.cuda.is_available():
+            pytest.skip("a GPU is present")
+    except Exception:
+        pass
+    import numpy as np
+    t = [np.ones((1, 2, 2)), np.ones((2, 2, 1))]
+    for call in (lambda: ttg.soft_threshold(t, 0.5), lambda: ttg.left_orthogonalize(t),
+                 lambda: ttg.frob_norm_apply([np.ones((1, 2, 2, 1))], [np.ones((1, 2, 1))])):
+        with pytest.raises(ttg.TTGError) as e:
+            call()
+        assert e.value.status == 9
