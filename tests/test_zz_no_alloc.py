@@ -9,8 +9,9 @@ These tests call it through the C-ABI and compare it with the allocating
 entry point ttg_round on the same inputs, at the tolerance the other GPU
 tests use, on two calls in a row (the array is shared and keeps the last
 call's contents, so the second call checks that every call starts clean).
-This file is collected last so that a stop at its first failure has
-already run every other test.
+This file is collected after the parity suites (only the full-size checks
+of test_zzz_full_size.py follow) so that a stop at its first failure has
+already run them.
 """
 import ctypes as C
 
