@@ -56,6 +56,17 @@ def main():
     idx = np.random.default_rng(49).integers(0, 4, size=(64, 32)).astype(np.int32)
     out["cfg4b_idx"] = idx
     out["cfg4b_values"] = O.eval_batch(t4b, idx)
+    # soft_threshold (round/tt_soft_threshold.hpp:42-178) of a small TT, and
+    # frob_norm_apply (algebra/tt_matrix_frob_norm_apply.hpp:36-98) of the
+    # reference test's matvec and matmat cases.
+    t5 = O.random([3, 4, 5, 3], 6, 99)
+    s5 = O.soft_threshold(t5, 0.05 * O.norm(t5))
+    out["soft_ranks"] = np.array(O.ranks(s5))
+    out["soft_dense"] = O.to_dense(s5)
+    A6 = O.random_matrix([4, 3, 4, 2], [3, 4, 2, 3], 4, 0xBEEF01)
+    x6 = O.random([3, 4, 2, 3], 3, 0xDEAD02)
+    B6 = O.random_matrix([3, 4, 2, 3], [4, 3, 4, 2], 2, 0xDEAD02)
+    out["frob_apply"] = np.array([O.frob_norm_apply(A6, x6), O.frob_norm_apply(A6, B6)])
     np.savez_compressed(os.path.join(HERE, "oracle_golden.npz"), **out)
     print("wrote", os.path.join(HERE, "oracle_golden.npz"))
 

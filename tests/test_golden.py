@@ -49,6 +49,16 @@ def test_oracle_reproduces_golden():
     t4b = O.random([4] * 32, 64, 48, fan_in_scale=True)
     v = O.eval_batch(t4b, G["cfg4b_idx"])
     assert np.allclose(v, G["cfg4b_values"], rtol=1e-13, atol=0)
+    t5 = O.random([3, 4, 5, 3], 6, 99)
+    s5 = O.soft_threshold(t5, 0.05 * O.norm(t5))
+    assert O.ranks(s5) == list(G["soft_ranks"])
+    ref = G["soft_dense"]
+    assert np.linalg.norm(O.to_dense(s5) - ref) <= 1e-13 * np.linalg.norm(ref)
+    A6 = O.random_matrix([4, 3, 4, 2], [3, 4, 2, 3], 4, 0xBEEF01)
+    x6 = O.random([3, 4, 2, 3], 3, 0xDEAD02)
+    B6 = O.random_matrix([3, 4, 2, 3], [4, 3, 4, 2], 2, 0xDEAD02)
+    f = [O.frob_norm_apply(A6, x6), O.frob_norm_apply(A6, B6)]
+    assert np.allclose(f, G["frob_apply"], rtol=1e-13, atol=0)
 
 
 @pytest.mark.gpu
