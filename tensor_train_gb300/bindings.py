@@ -37,7 +37,7 @@ from . import round_method as _method
 from . import schedule as _schedule
 
 __all__ = [
-    "RoundOptions", "RoundResult", "TTCore", "TTCoreMatrix", "TensorTrain",
+    "RoundOptions", "RoundResult", "TTCore", "TTCoreMatrix", "TTGError", "TensorTrain",
     "TensorTrainMatrix", "canonical_unit", "from_dense", "from_samples", "neg", "neg_matrix",
     "ones", "random", "round_gauge", "round_method", "zeros",
 ]
@@ -562,5 +562,3 @@ def from_dense(data, shape, eps=None, opts=None, **kwargs):
 def from_samples(func, shape, opts=None, **kwargs):
     raise NotImplementedError("cross approximation is outside the rounding path")
 
-
-TTGError = TTGError
