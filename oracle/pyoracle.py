@@ -75,6 +75,8 @@ def lib():
         "ttor_norm": (C.c_int, [_P, _DP]),
         "ttor_norm_qr": (C.c_double, [_P]),
         "ttor_frob_norm_apply": (C.c_int, [_P, _P, _DP]),
+        "ttor_round_iter": (_P, [_P, C.c_int, C.c_double, C.c_int, C.c_int, C.c_double,
+                                 C.c_ulonglong, _P, C.c_int, _IP, _DP]),
         "ttor_apply_core": (C.c_int, [C.c_int, _DP, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int,
                                       _DP, C.c_int, C.c_int, C.c_int, _DP, _DP]),
         "ttor_soft_threshold": (_P, [_P, C.c_double]),
@@ -315,6 +317,32 @@ def apply_core(A, X, F=None):
         raise OracleError(lib().ttor_last_error().decode())
     shp = (alpha, m, b * bx) if X.ndim == 3 else (alpha, m, nout, b * bx)
     return out.reshape(shp)
+
+
+def round_iter(a, method, eps=0.0, max_rank=0, max_iters=20, tol=1e-12, seed=0, warm=None,
+               cold_random=False):
+    """ALS (method "als") or two-site DMRG ("dmrg") rounding
+    (round/tt_als.hpp, round/tt_dmrg.hpp); returns (cores, info) with info =
+    {"iters_run", "converged", "final_change"}."""
+    ha = H(a)
+    hw = H(warm) if warm is not None else None
+    info = np.zeros(2, np.int32)
+    ch = C.c_double()
+    h = lib().ttor_round_iter(ha.h, 4 if method == "dmrg" else 3, float(eps), int(max_rank),
+                              int(max_iters), float(tol), int(seed), hw.h if hw else None,
+                              int(bool(cold_random)), info.ctypes.data_as(_IP), C.byref(ch))
+    out = Handle(h).cores()
+    return out, {"iters_run": int(info[0]), "converged": bool(info[1]),
+                 "final_change": ch.value}
+
+
+def apply_round_iter(A, x, method, **kw):
+    """matvec_/matmat_ als / dmrg round (round/tt_matvec_als_round.hpp,
+    tt_matvec_dmrg_round.hpp, tt_matmat_als_round.hpp,
+    tt_matmat_dmrg_round.hpp): the product, then the iterative rounder with
+    a random cold start."""
+    y = matmat(A, x) if x and x[0].ndim == 4 else matvec(A, x)
+    return round_iter(y, method, cold_random=True, **kw)
 
 
 def soft_threshold(a, tau=0.0):

@@ -1448,4 +1448,400 @@ inline TT random_uneven(uint64_t seed, int dmin, int dmax, int rmin, int rmax)
   return t;
 }
 
+// ---------------------------------------------------------------------------
+// Iterative rounding: ALS and two-site DMRG (round/tt_als.hpp:27-306,
+// round/tt_dmrg.hpp:27-309, detail/als_local_solve.hpp,
+// detail/dmrg_local_solve.hpp, detail/warm_start.hpp).  Environments are
+// the inner-product chains of X against Y from both ends; a local update
+// solves for one core (ALS) or a merged pair (DMRG) in the mixed-canonical
+// gauge.  Convergence: max over bonds of the relative change of the bond's
+// singular values between sweeps.
+// ---------------------------------------------------------------------------
+struct IterOptions
+{
+  int max_rank = 0;       // 0: ALS derives it from an SVD round at eps
+  double eps = 0.0;
+  int max_iters = 20;
+  double tol = 1.0e-12;
+  uint64_t seed = 0;      // random cold start of the apply variants
+  const TT* warm = nullptr;
+};
+
+struct IterResult
+{
+  int iters_run = 0;
+  double final_change = 0.0;
+  bool converged = false;
+};
+
+// contract_inner_step_right (detail/contract.hpp:90-139): F (ca.rp x cb.rp)
+// -> F' (ca.r x cb.r) = sum over (i, a', b') ca(a, i, a') F(a', b') cb(b, i, b').
+inline Mat contract_inner_step_right(const Core& ca, const Core& cb, const Mat& F)
+{
+  if (ca.n != cb.n)
+    fail("contract_inner_step_right: n_phys mismatch");
+  if (F.rows != ca.rp || F.cols != cb.rp)
+    fail("contract_inner_step_right: environment shape mismatch");
+  const int64_t rows = static_cast<int64_t>(ca.r) * ca.n;
+  Mat T1(rows, cb.rp);
+  gemm_nn(rows, cb.rp, ca.rp, ca.v.data(), ca.rp, F.data(), F.cols, T1.data(), T1.cols);
+  // F' = T1 viewed as (ca.r, n*cb.rp) times right_unfold(cb)^T.
+  const int64_t w = static_cast<int64_t>(ca.n) * cb.rp;
+  Mat out(ca.r, cb.r);
+  for (int a = 0; a < ca.r; ++a)
+    for (int b = 0; b < cb.r; ++b)
+    {
+      double acc = 0.0;
+      const double* t = &T1.v[static_cast<size_t>(a) * w];
+      const double* c = &cb.v[static_cast<size_t>(b) * w];
+      for (int64_t j = 0; j < w; ++j)
+        acc += t[j] * c[j];
+      out(a, b) = acc;
+    }
+  return out;
+}
+
+// als_local_update (detail/als_local_solve.hpp): X_k = L Y_k R as a core
+// (L.rows, n, R.cols).
+inline Core als_local_update(const Mat& L, const Core& Yk, const Mat& R)
+{
+  const int64_t w1 = static_cast<int64_t>(Yk.n) * Yk.rp;
+  Mat T1(L.rows, w1);
+  gemm_nn(L.rows, w1, Yk.r, L.data(), L.cols, Yk.v.data(), w1, T1.data(), w1);
+  Core X(static_cast<int>(L.rows), Yk.n, static_cast<int>(R.cols));
+  gemm_nn(L.rows * Yk.n, R.cols, Yk.rp, T1.data(), Yk.rp, R.data(), R.cols, X.v.data(), R.cols);
+  return X;
+}
+
+inline std::vector<double> core_singular_values(const Core& c)
+{
+  Mat U, Vt;
+  std::vector<double> s;
+  svd_thin(c.v.data(), static_cast<int64_t>(c.r) * c.n, c.rp, U, s, Vt);
+  return s;
+}
+
+// Max over bonds of ||s_now - s_prev|| / ||s_now||; a bond whose size
+// changed sets the running value to 1.
+inline double sv_change(const std::vector<std::vector<double>>& now,
+                        const std::vector<std::vector<double>>& prev)
+{
+  double worst = 0.0;
+  for (size_t k = 0; k < now.size(); ++k)
+  {
+    if (now[k].size() != prev[k].size())
+    {
+      worst = 1.0;  // overwrite, as the reference does (tt_als.hpp:182-186)
+      continue;
+    }
+    double dn = 0.0, nn = 0.0;
+    for (size_t i = 0; i < now[k].size(); ++i)
+    {
+      dn += (now[k][i] - prev[k][i]) * (now[k][i] - prev[k][i]);
+      nn += now[k][i] * now[k][i];
+    }
+    worst = std::max(worst, std::sqrt(dn) / (std::sqrt(nn) + 1.0e-300));
+  }
+  return worst;
+}
+
+// als_engine (round/tt_als.hpp:52-206).
+inline TT als_engine(const TT& Y, TT X, const IterOptions& o, IterResult* info,
+                     bool x_right_canonical)
+{
+  const int d = Y.d();
+  if (d <= 1)
+  {
+    if (info)
+      *info = IterResult{0, 0.0, true};
+    TT out;
+    if (d == 1)
+      out.c.push_back(Y.c[0]);
+    return out;
+  }
+  if (!x_right_canonical)
+    right_orthogonalize(X);
+  std::vector<Mat> R(static_cast<size_t>(d + 1)), L(static_cast<size_t>(d + 1));
+  R[d] = Mat(1, 1);
+  R[d](0, 0) = 1.0;
+  for (int k = d - 1; k >= 1; --k)
+    R[k] = contract_inner_step_right(Y.c[k], X.c[k], R[k + 1]);
+  L[0] = Mat(1, 1);
+  L[0](0, 0) = 1.0;
+  std::vector<std::vector<double>> s_prev;
+  double change = 0.0;
+  bool converged = false;
+  int iters = 0;
+  for (int it = 0; it < o.max_iters; ++it)
+  {
+    for (int k = 0; k < d; ++k)
+    {
+      X.c[k] = als_local_update(L[k], Y.c[k], R[k + 1]);
+      if (k < d - 1)
+      {
+        left_qr_step(X.c[k], X.c[k + 1]);
+        L[k + 1] = contract_inner_step(L[k], X.c[k], Y.c[k]);
+      }
+    }
+    for (int k = d - 1; k >= 0; --k)
+    {
+      if (k < d - 1)
+        X.c[k] = als_local_update(L[k], Y.c[k], R[k + 1]);
+      if (k > 0)
+      {
+        right_qr_step(X.c[k], X.c[k - 1]);
+        R[k] = contract_inner_step_right(Y.c[k], X.c[k], R[k + 1]);
+      }
+    }
+    ++iters;
+    std::vector<std::vector<double>> s_now;
+    for (int k = 0; k < d - 1; ++k)
+      s_now.push_back(core_singular_values(X.c[k]));
+    change = s_prev.empty() ? 1.0 : sv_change(s_now, s_prev);
+    s_prev = std::move(s_now);
+    if (change <= o.tol)
+    {
+      converged = true;
+      break;
+    }
+  }
+  if (info)
+    *info = IterResult{iters, change, converged};
+  return X;
+}
+
+// warm_start_tt_compatible (detail/warm_start.hpp): same length and modes.
+inline bool warm_compatible(const TT* w, const TT& ref)
+{
+  if (!w || w->d() != ref.d())
+    return false;
+  for (int k = 0; k < ref.d(); ++k)
+    if (w->c[k].n != ref.c[k].n)
+      return false;
+  if (w->matrix != ref.matrix)
+    return false;
+  if (ref.matrix)
+    for (int k = 0; k < ref.d(); ++k)
+      if (w->mrow[k] != ref.mrow[k] || w->ncol[k] != ref.ncol[k])
+        return false;
+  return true;
+}
+
+inline int tt_max_rank(const TT& t)
+{
+  int m = 0;
+  for (int r : t.ranks())
+    m = std::max(m, r);
+  return m;
+}
+
+inline TT as_packed(TT t)
+{
+  t.matrix = false;
+  t.mrow.clear();
+  t.ncol.clear();
+  return t;
+}
+
+inline TT as_matrix_like(TT t, const TT& like)
+{
+  t.matrix = like.matrix;
+  t.mrow = like.mrow;
+  t.ncol = like.ncol;
+  return t;
+}
+
+// als_round (round/tt_als.hpp:212-300) of a TT, or of a TT-matrix through
+// its packed 3-axis cores (round/tt_matrix_als_round.hpp).  cold_random:
+// the apply variants start from random(shape, max_rank, seed) instead of
+// round_right_canonical (round/tt_matvec_als_round.hpp:88-95,
+// round/tt_matmat_als_round.hpp).
+inline TT als_round(const TT& Yin, IterOptions o, IterResult* info, bool cold_random = false)
+{
+  if (std::isnan(o.eps))
+    fail("als_round: eps is NaN; must be a valid number");
+  const TT Y = as_packed(Yin);
+  const int d = Y.d();
+  if (d <= 1)
+  {
+    if (info)
+      *info = IterResult{0, 0.0, true};
+    return as_matrix_like(round(Y, o.eps, o.max_rank), Yin);
+  }
+  TT svd_ref;
+  TT warm_packed;
+  const TT* warm = nullptr;
+  if (o.warm && warm_compatible(o.warm, Yin))
+  {
+    warm_packed = as_packed(*o.warm);
+    warm = &warm_packed;
+  }
+  if (o.max_rank <= 0)
+  {
+    if (o.eps <= 0.0)
+      fail("als_round: max_rank <= 0 and eps <= 0; ALS requires either max_rank > 0 or "
+           "eps > 0 to determine compression target");
+    svd_ref = round(Y, o.eps, 0);
+    o.max_rank = tt_max_rank(svd_ref);
+    if (!warm)
+      warm = &svd_ref;
+  }
+  if (warm)
+    for (int r : warm->ranks())
+      if (r > o.max_rank)
+        fail("als_round: warm_start max rank " + std::to_string(r) + " exceeds max_rank " +
+             std::to_string(o.max_rank));
+  TT X0;
+  bool rc = false;
+  if (warm)
+    X0 = *warm;
+  else if (cold_random)
+    X0 = random(Y.shape(), o.max_rank, o.seed);
+  else
+  {
+    X0 = round_right_canonical(Y, 0.0, o.max_rank);
+    rc = true;
+  }
+  return as_matrix_like(als_engine(Y, std::move(X0), o, info, rc), Yin);
+}
+
+// merge_y_block (detail/dmrg_local_solve.hpp): Theta (rXl*n_k, n_k1*rXr) =
+// (L Y_k) (Y_k1 R) with the middle bond of Y contracted.
+inline Mat merge_y_block(const Mat& L, const Core& Yk, const Core& Yk1, const Mat& R)
+{
+  const int64_t w1 = static_cast<int64_t>(Yk.n) * Yk.rp;
+  Mat T1(L.rows, w1);
+  gemm_nn(L.rows, w1, Yk.r, L.data(), L.cols, Yk.v.data(), w1, T1.data(), w1);
+  const int64_t h2 = static_cast<int64_t>(Yk1.r) * Yk1.n;
+  Mat T2(h2, R.cols);
+  gemm_nn(h2, R.cols, Yk1.rp, Yk1.v.data(), Yk1.rp, R.data(), R.cols, T2.data(), R.cols);
+  const int64_t rows = L.rows * Yk.n, cols = static_cast<int64_t>(Yk1.n) * R.cols;
+  Mat Th(rows, cols);
+  gemm_nn(rows, cols, Yk.rp, T1.data(), Yk.rp, T2.data(), cols, Th.data(), cols);
+  return Th;
+}
+
+// split_two_site_lr / _rl (detail/dmrg_local_solve.hpp): truncated SVD of
+// Theta; lr: X_k <- U, X_k1 <- diag(s) V^T (s_head receives s[:r]);
+// rl: X_k <- U diag(s), X_k1 <- V^T.
+inline int split_two_site(const Mat& Th, int rXl, int nk, int nk1, int rXr, double delta,
+                          int max_rank, bool left_to_right, Core& Xk, Core& Xk1,
+                          std::vector<double>* s_head)
+{
+  Mat U, Vt;
+  std::vector<double> s;
+  svd_thin(Th.data(), Th.rows, Th.cols, U, s, Vt);
+  const int r = truncate_eps_rank(s, delta, max_rank);
+  Core a(rXl, nk, r), b(r, nk1, rXr);
+  for (int64_t i = 0; i < Th.rows; ++i)
+    for (int j = 0; j < r; ++j)
+      a.v[static_cast<size_t>(i * r + j)] = left_to_right ? U(i, j) : U(i, j) * s[j];
+  for (int j = 0; j < r; ++j)
+    for (int64_t q = 0; q < Th.cols; ++q)
+      b.v[static_cast<size_t>(j * Th.cols + q)] = left_to_right ? s[j] * Vt(j, q) : Vt(j, q);
+  Xk = std::move(a);
+  Xk1 = std::move(b);
+  if (s_head)
+    s_head->assign(s.begin(), s.begin() + r);
+  return r;
+}
+
+// dmrg_engine (round/tt_dmrg.hpp:45-212).
+inline TT dmrg_engine(const TT& Y, TT X, const IterOptions& o, IterResult* info,
+                      bool x_right_canonical)
+{
+  const int d = Y.d();
+  if (d <= 1)
+  {
+    if (info)
+      *info = IterResult{0, 0.0, true};
+    TT out;
+    if (d == 1)
+      out.c.push_back(Y.c[0]);
+    return out;
+  }
+  if (!x_right_canonical)
+    right_orthogonalize(X);
+  const double y_norm = std::sqrt(std::max(inner(Y, Y), 0.0));
+  const double delta = o.eps * y_norm / std::sqrt(static_cast<double>(std::max(d - 1, 1)));
+  std::vector<Mat> R(static_cast<size_t>(d + 1)), L(static_cast<size_t>(d + 1));
+  R[d] = Mat(1, 1);
+  R[d](0, 0) = 1.0;
+  for (int k = d - 1; k >= 1; --k)
+    R[k] = contract_inner_step_right(Y.c[k], X.c[k], R[k + 1]);
+  L[0] = Mat(1, 1);
+  L[0](0, 0) = 1.0;
+  std::vector<std::vector<double>> s_prev, s_now(static_cast<size_t>(d - 1));
+  double change = 0.0;
+  bool converged = false;
+  int iters = 0;
+  for (int it = 0; it < o.max_iters; ++it)
+  {
+    for (int k = 0; k < d - 1; ++k)
+    {
+      const Mat Th = merge_y_block(L[k], Y.c[k], Y.c[k + 1], R[k + 2]);
+      split_two_site(Th, static_cast<int>(L[k].rows), Y.c[k].n, Y.c[k + 1].n,
+                     static_cast<int>(R[k + 2].cols), delta, o.max_rank, true, X.c[k],
+                     X.c[k + 1], &s_now[k]);
+      L[k + 1] = contract_inner_step(L[k], X.c[k], Y.c[k]);
+    }
+    for (int k = d - 2; k >= 0; --k)
+    {
+      const Mat Th = merge_y_block(L[k], Y.c[k], Y.c[k + 1], R[k + 2]);
+      split_two_site(Th, static_cast<int>(L[k].rows), Y.c[k].n, Y.c[k + 1].n,
+                     static_cast<int>(R[k + 2].cols), delta, o.max_rank, false, X.c[k],
+                     X.c[k + 1], nullptr);
+      R[k + 1] = contract_inner_step_right(Y.c[k + 1], X.c[k + 1], R[k + 2]);
+    }
+    ++iters;
+    change = s_prev.empty() ? 1.0 : sv_change(s_now, s_prev);
+    s_prev = s_now;
+    if (change <= o.tol)
+    {
+      converged = true;
+      break;
+    }
+  }
+  if (info)
+    *info = IterResult{iters, change, converged};
+  return X;
+}
+
+// dmrg_round (round/tt_dmrg.hpp:217-300), and through packed cores
+// (round/tt_matrix_dmrg_round.hpp).  cold_random as for als_round
+// (round/tt_matvec_dmrg_round.hpp: random start when max_rank > 0).
+inline TT dmrg_round(const TT& Yin, const IterOptions& o, IterResult* info,
+                     bool cold_random = false)
+{
+  if (std::isnan(o.eps) || o.eps <= 0.0)
+    fail("dmrg_round: eps must be > 0 for DMRG compression");
+  const TT Y = as_packed(Yin);
+  const int d = Y.d();
+  if (d <= 1)
+  {
+    if (info)
+      *info = IterResult{0, 0.0, true};
+    return as_matrix_like(round(Y, o.eps, o.max_rank), Yin);
+  }
+  TT X0;
+  bool rc = false;
+  if (o.warm && warm_compatible(o.warm, Yin))
+  {
+    X0 = as_packed(*o.warm);
+    if (o.max_rank > 0)
+      for (int r : X0.ranks())
+        if (r > o.max_rank)
+          fail("dmrg_round: warm_start max rank " + std::to_string(r) + " exceeds max_rank " +
+               std::to_string(o.max_rank));
+  }
+  else if (cold_random && o.max_rank > 0)
+    X0 = random(Y.shape(), o.max_rank, o.seed);
+  else
+  {
+    X0 = round_right_canonical(Y, o.eps, o.max_rank);
+    rc = true;
+  }
+  return as_matrix_like(dmrg_engine(Y, std::move(X0), o, info, rc), Yin);
+}
+
 }  // namespace ttor

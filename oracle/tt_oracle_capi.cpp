@@ -267,6 +267,31 @@ int ttor_apply_core(int fused, const double* F, int alpha, int a, int m, int p, 
   }) ? 0 : -1;
 }
 
+// Iterative rounding: method 3 = ALS, 4 = DMRG (round/round.hpp:237-250).
+// warm may be NULL; cold_random = 1 starts from random(shape, max_rank,
+// seed) as the apply variants do.  info = {iters_run, converged} and change.
+ttor_tt* ttor_round_iter(const ttor_tt* a, int method, double eps, int max_rank, int max_iters,
+                         double tol, unsigned long long seed, const ttor_tt* warm,
+                         int cold_random, int* info, double* change)
+{
+  return guard([&]() -> ttor_tt* {
+    IterOptions o;
+    o.eps = eps;
+    o.max_rank = max_rank;
+    o.max_iters = max_iters;
+    o.tol = tol;
+    o.seed = seed;
+    o.warm = warm ? &warm->t : nullptr;
+    IterResult r;
+    TT y = method == 4 ? dmrg_round(a->t, o, &r, cold_random != 0)
+                       : als_round(a->t, o, &r, cold_random != 0);
+    info[0] = r.iters_run;
+    info[1] = r.converged ? 1 : 0;
+    *change = r.final_change;
+    return new ttor_tt{std::move(y)};
+  });
+}
+
 int ttor_frob_norm_apply(const ttor_tt* A, const ttor_tt* x, double* out)
 {
   return guard([&]() -> int {
