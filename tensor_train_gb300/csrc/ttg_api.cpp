@@ -1399,6 +1399,14 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
     return fail(TTG_ERR_METHOD, std::string(op) +
                                     ": round_method::svd_streaming / svd_naive are only valid on "
                                     "matvec_round / matmat_round respectively.");
+  // Shapes first: an invalid tensor is an argument error with or without a
+  // device (the reference aborts on it before any arithmetic).
+  for (int32_t i = 0; i < count; ++i)
+  {
+    Shape s;
+    if (int32_t st = describe(&ins[i], op, s))
+      return st;
+  }
   if (int32_t st = need_device())
     return st;
   std::lock_guard<std::mutex> lk(g_mu);
@@ -1455,6 +1463,11 @@ int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   g_err.clear();
   if (!in || !out)
     return fail(TTG_ERR_ARG, "right_orthogonalize: null argument");
+  {
+    Shape s;
+    if (int32_t st = describe(in, "right_orthogonalize", s))
+      return st;
+  }
   if (int32_t st = need_device())
     return st;
   std::lock_guard<std::mutex> lk(g_mu);
@@ -1477,6 +1490,11 @@ int32_t ttg_left_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   g_err.clear();
   if (!in || !out)
     return fail(TTG_ERR_ARG, "left_orthogonalize: null argument");
+  {
+    Shape s;
+    if (int32_t st = describe(in, "left_orthogonalize", s))
+      return st;
+  }
   if (int32_t st = need_device())
     return st;
   std::lock_guard<std::mutex> lk(g_mu);

@@ -112,3 +112,23 @@ def test_no_silent_cpu_fallback_new_entries(ttg):
         with pytest.raises(ttg.TTGError) as e:
             call()
         assert e.value.status == 9
+
+
+def test_shape_errors_before_device_work(ttg):
+    # types/tt.hpp:35-70 (r_0 = r_d = 1, matching bonds) and
+    # detail/shape_check.hpp: an invalid TT is refused whether or not a
+    # device is present
+    import numpy as np
+    bad_bond = [np.ones((1, 2, 3)), np.ones((2, 2, 1))]     # 3 vs 2 at bond 1
+    bad_r0 = [np.ones((2, 2, 1))]
+    bad_rd = [np.ones((1, 2, 2))]
+    for t in (bad_bond, bad_r0, bad_rd):
+        for call in (lambda: ttg.round(t, ttg.RoundOptions(eps=1e-8)),
+                     lambda: ttg.round_batch([t], ttg.RoundOptions(eps=1e-8)),
+                     lambda: ttg.right_orthogonalize(t),
+                     lambda: ttg.left_orthogonalize(t),
+                     lambda: ttg.soft_threshold(t, 0.5),
+                     lambda: ttg.inner(t, t)):
+            with pytest.raises(ttg.TTGError) as e:
+                call()
+            assert e.value.status == 2, e.value
