@@ -87,3 +87,24 @@ def test_core_layout_and_tt_container():
     assert T.d == 2 and T.shape == [2, 3] and T.ranks == [1, 1, 1]
     assert T.max_rank == 1 and T.num_params == 5
     np.testing.assert_allclose(T.to_dense(), [10.0, 20.0, 30.0, 20.0, 40.0, 60.0], atol=1e-12)
+
+
+def test_tt_matrix_layout():
+    # tests/core/test_tt_matrix.cpp: one core, rank-1 and rank-2 two-site
+    # operators against their dense (row-major, I = i0*m1 + i1) matrices
+    m, n = 3, 4
+    dense = np.array([[1.0 + i * 10.0 + j for j in range(n)] for i in range(m)])
+    A = tt.TensorTrainMatrix.from_cores([dense.reshape(1, m, n, 1)])
+    assert A.total_rows == m and A.total_cols == n
+    np.testing.assert_array_equal(A.to_dense().reshape(m, n), dense)
+    m0, n0, m1, n1 = 2, 3, 3, 2
+    for rank in (1, 2):
+        Us = [np.array([0.1 * (s + 1) + 0.07 * k for k in range(m0 * n0)]).reshape(m0, n0)
+              for s in range(rank)]
+        Vs = [np.array([-0.2 * (s + 1) + 0.05 * k for k in range(m1 * n1)]).reshape(m1, n1)
+              for s in range(rank)]
+        c0 = np.stack(Us, axis=-1).reshape(1, m0, n0, rank)
+        c1 = np.stack(Vs, axis=0).reshape(rank, m1, n1, 1)
+        A = tt.TensorTrainMatrix.from_cores([c0, c1])
+        want = sum(np.kron(U, V) for U, V in zip(Us, Vs))
+        np.testing.assert_allclose(A.to_dense().reshape(m0 * m1, n0 * n1), want, atol=1e-14)
