@@ -21,3 +21,20 @@ def test_numpy_round_matches_oracle():
         assert O.rel_err(y, ref) <= 1e-11
         # left-orthogonal cores 0..d-2 after the sweep (up to the balancing scale)
         assert O.rel_err(y, t) <= eps * 1.01
+
+
+def test_numpy_round_edge_cases():
+    # max_rank caps (applied after eps), two sites, a zero TT and a rank-1 TT
+    t = O.add(O.random([4] * 6, 8, 5, fan_in_scale=True), O.random([4] * 6, 8, 6, fan_in_scale=True))
+    for cap in (1, 3, 7):
+        y, ref = NR.round_tt(t, 1e-8, cap), O.round(t, 1e-8, max_rank=cap)
+        assert O.ranks(y) == O.ranks(ref) and max(O.ranks(y)) <= cap
+        assert O.rel_err(y, ref) <= 1e-10
+    two = O.random([6, 7], 5, 3)
+    assert O.rel_err(NR.round_tt(two, 1e-12), O.round(two, 1e-12)) <= 1e-12
+    z = NR.round_tt(O.zeros([3, 4, 2]), 1e-8)
+    assert O.ranks(z) == [1, 1, 1, 1] and all(np.all(c == 0) for c in z)
+    one = O.ones([3, 4, 5])
+    y = NR.round_tt(one, 1e-10)
+    assert O.ranks(y) == O.ranks(O.round(one, 1e-10)) == [1, 1, 1, 1]
+    assert O.rel_err(y, one) <= 1e-14
