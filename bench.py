@@ -156,6 +156,33 @@ class Clocks:
                 "samples": len(sm)}
 
 
+THROTTLE_REASONS = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown")
+
+
+def clocks_ok(summary, floor=0.85):
+    """A timed region counts when no thermal or hardware slowdown was active
+    and the median SM clock under load is not stuck well below its maximum
+    without a reason (a leftover clock lock).  sw_power_cap is allowed."""
+    reasons = set(summary.get("reasons") or [])
+    if reasons & set(THROTTLE_REASONS):
+        return False
+    sm, smax = summary.get("sm_mhz"), summary.get("sm_max_mhz")
+    if sm and smax and sm < floor * smax and "sw_power_cap" not in reasons:
+        return False
+    return True
+
+
+def any_rank(flag, world, device="cuda"):
+    """True on every rank when `flag` is true on any rank (so that all ranks
+    take the same branch before the next collective)."""
+    if world <= 1:
+        return bool(flag)
+    import torch
+    t = torch.tensor([1.0 if flag else 0.0], device=device, dtype=torch.float64)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return bool(t.item() > 0.0)
+
+
 def dist_setup(gpus):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -217,20 +244,29 @@ def run_ours(args):
         torch.cuda.synchronize()
         outs = plan.download(sptr)
         bad = [r.status for r in plan.results if r.status != 0]
-        launches0 = T.kernel_launches()
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        barrier()
-        torch.cuda.synchronize()
-        with Clocks(local) as clk:
-            ev0.record(stream)
-            for _ in range(args.steps):
-                plan.run(sptr)
-            ev1.record(stream)
+
+        def timed_region():
+            launches0 = T.kernel_launches()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            barrier()
             torch.cuda.synchronize()
-        barrier()
-        launches = T.kernel_launches() - launches0
-        ms_total = max_over_ranks(ev0.elapsed_time(ev1), world)
+            with Clocks(local) as clk:
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    plan.run(sptr)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+            barrier()
+            return (T.kernel_launches() - launches0,
+                    max_over_ranks(ev0.elapsed_time(ev1), world), clk.summary())
+
+        launches, ms_total, clocks = timed_region()
+        # A region that ran throttled or under a clock lock is measured once more.
+        remeasured = any_rank(not clocks_ok(clocks), world)
+        if remeasured:
+            launches, ms_total, clocks = timed_region()
+        clocks["remeasured"] = remeasured
         kms = []
         for _ in range(3):
             plan.run(sptr)
@@ -240,7 +276,7 @@ def run_ours(args):
         ms_step = ms_total / args.steps
         return {"opts": opts, "outs": outs, "bad": len(bad), "launches": launches, "tuned": tuned,
                 "ms_step": ms_step, "value": count * world / (ms_step / 1e3),
-                "kernel_ms": statistics.mean(kms), "clocks": clk.summary(), "io": io}
+                "kernel_ms": statistics.mean(kms), "clocks": clocks, "io": io}
 
     plain = measure(T.precision.fp64)
     mixed = measure(T.precision.mixed)

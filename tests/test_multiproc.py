@@ -24,12 +24,14 @@ def _worker(rank, world, port, q):
     r, w, _ = bench.dist_setup(world)
     base = bench.shard_base(r, 4096)
     t = bench.max_over_ranks(10.0 + 5.0 * r, w, device="cpu")
+    # a throttled region on one rank makes every rank measure again
+    again = (bench.any_rank(r == 1, w, device="cpu"), bench.any_rank(False, w, device="cpu"))
     # every rank's seeds are disjoint from the others'
     seeds = set(range(base, base + 4096))
     gathered = [None] * w
     dist.all_gather_object(gathered, sorted(seeds)[:1] + sorted(seeds)[-1:])
     dist.destroy_process_group()
-    q.put((r, w, base, t, gathered))
+    q.put((r, w, base, t, gathered, again))
 
 
 def test_two_gloo_ranks_shard_and_reduce():
@@ -43,7 +45,8 @@ def test_two_gloo_ranks_shard_and_reduce():
     for p in procs:
         p.join(timeout=60)
         assert p.exitcode == 0
-    (r0, w0, b0, t0, g0), (r1, w1, b1, t1, g1) = out
+    (r0, w0, b0, t0, g0, a0), (r1, w1, b1, t1, g1, a1) = out
+    assert a0 == a1 == (True, False)
     assert (r0, r1, w0, w1) == (0, 1, 2, 2)
     assert b1 - b0 == 4096                 # disjoint seed ranges
     assert t0 == t1 == 15.0                # the job's time is the slowest rank's
@@ -60,3 +63,12 @@ def test_reference_arm_runs_on_rank0_only(monkeypatch, capsys):
     args = argparse.Namespace(gpus=2, steps=1, warmup=0, count=8)
     bench.run_reference(args)          # returns before any work on rank 1
     assert capsys.readouterr().out == ""
+
+
+def test_clock_screen():
+    import bench
+    assert bench.clocks_ok({"sm_mhz": 2070, "sm_max_mhz": 2070, "reasons": []})
+    assert bench.clocks_ok({"sm_mhz": 1700, "sm_max_mhz": 2070, "reasons": ["sw_power_cap"]})
+    for r in bench.THROTTLE_REASONS:
+        assert not bench.clocks_ok({"sm_mhz": 2070, "sm_max_mhz": 2070, "reasons": [r]})
+    assert not bench.clocks_ok({"sm_mhz": 1200, "sm_max_mhz": 2070, "reasons": []})  # clock lock
