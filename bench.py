@@ -488,15 +488,20 @@ def run_single(args):
             plan.run(sptr)
         torch.cuda.synchronize()
         ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        launches0 = T.kernel_launches()
-        with Clocks(0) as clk:
-            ev0.record(stream)
-            for _ in range(args.steps):
-                plan.run(sptr)
-            ev1.record(stream)
-            torch.cuda.synchronize()
-        plan.launches = T.kernel_launches() - launches0
-        return ev0.elapsed_time(ev1) / args.steps, clk.summary()
+        for attempt in range(2):
+            launches0 = T.kernel_launches()
+            with Clocks(0) as clk:
+                ev0.record(stream)
+                for _ in range(args.steps):
+                    plan.run(sptr)
+                ev1.record(stream)
+                torch.cuda.synchronize()
+            plan.launches = T.kernel_launches() - launches0
+            clocks = clk.summary()
+            clocks["remeasured"] = attempt > 0
+            if clocks_ok(clocks):
+                break
+        return ev0.elapsed_time(ev1) / args.steps, clocks
 
     def e2e(call, nbytes_in, out_bytes):
         """The public host-buffer call (numpy in, numpy out: pack, H2D,

@@ -72,3 +72,17 @@ def test_clock_screen():
     for r in bench.THROTTLE_REASONS:
         assert not bench.clocks_ok({"sm_mhz": 2070, "sm_max_mhz": 2070, "reasons": [r]})
     assert not bench.clocks_ok({"sm_mhz": 1200, "sm_max_mhz": 2070, "reasons": []})  # clock lock
+
+
+def test_clock_sample_parsing():
+    import bench
+    c = bench.Clocks(0)
+    c.lines = ["0, 2070, 2070, 900.1, Not Active, Not Active, Not Active, Not Active, Not Active",
+               "0, 2055, 2070, 1390.0, Active, Not Active, Not Active, Not Active, Active",
+               "garbage"]
+    s = c.summary()
+    assert s["sm_max_mhz"] == 2070 and s["samples"] == 2 and s["reasons"] == ["sw_power_cap"]
+    assert bench.clocks_ok(s)
+    c.lines = ["0, 1100, 2070, 500.0, Active, Active, Not Active, Not Active, Not Active"]
+    s = c.summary()
+    assert s["reasons"] == ["hw_slowdown"] and not bench.clocks_ok(s)
