@@ -31,31 +31,58 @@ def gemm(m, k, n):
     return 2.0 * m * k * n
 
 
+def round_steps(modes, ranks_in, ranks_out):
+    """The step shapes of one round, in sweep order: ("rqr", m, c, r_eff,
+    h_prev) for the R->L QR steps and ("svd", rows, cols, r_new, w_next) for
+    the L->R truncation steps (the shapes the reference's sweep meets)."""
+    d = len(modes)
+    steps = []
+    if d <= 1:
+        return steps
+    n = list(modes)
+    r = list(ranks_in)
+    for k in range(d - 1, 0, -1):
+        m, c = n[k] * r[k + 1], r[k]
+        e = min(m, c)
+        steps.append(("rqr", m, c, e, r[k - 1] * n[k - 1]))
+        r[k] = e
+    for k in range(d - 1):
+        rows, cols = r[k] * n[k], r[k + 1]
+        rnew = ranks_out[k + 1]
+        steps.append(("svd", rows, cols, rnew, n[k + 1] * r[k + 2]))
+        r[k + 1] = rnew
+    return steps
+
+
 def round_flops(modes, ranks_in, ranks_out):
     """F_round of one TT with mode sizes `modes`, input ranks and output ranks."""
     d = len(modes)
     if d <= 1:
         return 0.0
-    n = list(modes)
-    r = list(ranks_in)
     F = 0.0
-    for k in range(d - 1, 0, -1):
-        m, c = n[k] * r[k + 1], r[k]
-        e = min(m, c)
-        F += qr(max(m, c), min(m, c)) + gemm(r[k - 1] * n[k - 1], r[k], e)
-        r[k] = e
-    F += 2.0 * r[0] * n[0] * r[1]
-    for k in range(d - 1):
-        rows, cols = r[k] * n[k], r[k + 1]
-        if rows >= 2 * cols:
-            F += qr(rows, cols) + svd_sq(cols) + gemm(rows, cols, cols)
+    for kind, a, b, c, w in round_steps(modes, ranks_in, ranks_out):
+        if kind == "rqr":
+            F += qr(max(a, b), min(a, b)) + gemm(w, b, c)
         else:
-            F += svd(rows, cols)
-        rnew = ranks_out[k + 1]
-        F += gemm(rnew, cols, n[k + 1] * r[k + 2])
-        r[k + 1] = rnew
-    F += 4.0 * sum(ranks_out[k] * n[k] * ranks_out[k + 1] for k in range(d))
+            rows, cols, rnew = a, b, c
+            if rows >= 2 * cols:
+                F += qr(rows, cols) + svd_sq(cols) + gemm(rows, cols, cols)
+            else:
+                F += svd(rows, cols)
+            F += gemm(rnew, cols, w)
+    F += 2.0 * _norm_entries(modes, ranks_in)
+    F += 4.0 * sum(ranks_out[k] * modes[k] * ranks_out[k + 1] for k in range(d))
     return F
+
+
+def _norm_entries(modes, ranks_in):
+    """Entries of core 0 after the R->L sweep: n_0 * r_1' with r_1' the
+    (possibly shrunk) first bond."""
+    r = list(ranks_in)
+    n = list(modes)
+    for k in range(len(n) - 1, 0, -1):
+        r[k] = min(n[k] * r[k + 1], r[k])
+    return r[0] * n[0] * r[1]
 
 
 def matvec_flops(A_ranks, x_ranks, m, n):
