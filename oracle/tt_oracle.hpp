@@ -17,10 +17,13 @@
 // reference file:line it follows (paths inside the reference project).
 //
 // Parity status: the reference ships no golden vectors; its tests are
-// known-answer-by-construction (dense equality, invariants).  Those tests are
-// restated against this oracle in tests/test_oracle.py.  Bitwise agreement
-// with Eigen is not claimed (QR/SVD sign conventions differ); results are
-// compared as tensors (relative Frobenius error) and as ranks.
+// known-answer-by-construction (dense equality, invariants).  Every one of
+// them on this path is restated against this oracle (tests/test_oracle*.py,
+// tests/test_bindings_reference.py), and two independent numpy/LAPACK
+// restatements (oracle/numpy_round.py, oracle/numpy_iter.py) agree with it.
+// Bitwise agreement with Eigen is not claimed (QR/SVD sign conventions
+// differ); results are compared as tensors (relative Frobenius error) and as
+// ranks.
 #pragma once
 
 #include <algorithm>
