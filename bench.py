@@ -33,10 +33,11 @@ EPS = 1e-8
 SEED0 = 1000
 
 
-def measured_peaks():
+def measured_peaks(path=None):
     """HBM GB/s and dense BF16 TFLOP/s measured on the GB300s
     (MEASURED_PEAKS.json beside this file), else the published fallback."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    if path is None:
+        path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
     try:
         with open(path) as f:
             d = json.load(f)

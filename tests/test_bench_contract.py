@@ -21,3 +21,16 @@ def test_reference_arm_line(capsys, monkeypatch):
     e2e = line["e2e"]
     assert e2e["h2d_bytes_per_step"] == 0 and e2e["d2h_bytes_per_step"] == 0
     assert e2e["unit"] == line["unit"]
+
+
+def test_roofline_objects(tmp_path):
+    import bench
+    hbm, bf16, src = bench.measured_peaks()
+    assert hbm > 0 and bf16 > 0
+    r = bench.roofline_tensor(6.5e11, 1000.0, 1.25, traffic=6e10)
+    assert r["bound"] == "tensor" and r["unit"] == "TFLOP/s" and r["peak"] == bf16
+    assert abs(r["achieved"] - 0.65) < 1e-12 and abs(r["frac"] - 0.65 / bf16) < 1e-15
+    assert abs(r["fp64_pipe"]["frac"] - 0.52) < 1e-12 and r["traffic"] == 6e10
+    # without the measured-peaks file: the published fallback, and it says so
+    hbm2, bf2, src2 = bench.measured_peaks(str(tmp_path / "absent.json"))
+    assert (hbm2, bf2) == (6800.0, 1900.0) and "fallback" in src2
