@@ -34,3 +34,26 @@ def test_roofline_objects(tmp_path):
     # without the measured-peaks file: the published fallback, and it says so
     hbm2, bf2, src2 = bench.measured_peaks(str(tmp_path / "absent.json"))
     assert (hbm2, bf2) == (6800.0, 1900.0) and "fallback" in src2
+
+
+def test_reference_arm_loads_only_the_oracle():
+    # The reference arm must not map the product library: it builds its
+    # inputs with the oracle's own generator and rounds them with the oracle.
+    import os
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    code = ("import argparse, sys, bench\n"
+            "bench.run_reference(argparse.Namespace(gpus=1, steps=1, warmup=0, count=4096))\n"
+            "assert 'tensor_train_gb300' not in sys.modules, 'product package imported'\n"
+            "maps = open('/proc/self/maps').read()\n"
+            "assert 'libttgpu' not in maps, 'product library mapped'\n")
+    env = dict(os.environ)
+    env.pop("RANK", None)
+    env.pop("WORLD_SIZE", None)
+    r = subprocess.run([sys.executable, "-c", code], cwd=root, env=env, capture_output=True,
+                       text=True, timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    import json
+    line = json.loads(r.stdout.strip().splitlines()[-1])
+    assert line["impl"] == "reference"

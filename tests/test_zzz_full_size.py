@@ -25,15 +25,21 @@ def test_round_d40_rank257(ttg, prec):
     assert rel <= 1e-10
 
 
-def test_batch_4096_uneven(ttg):
+@pytest.mark.parametrize("prec", ["mixed", "fp64"])
+def test_batch_4096_uneven(ttg, prec):
     with ThreadPoolExecutor(16) as ex:
         ts = list(ex.map(lambda i: ttg.random_uneven(1000 + i), range(4096)))
-    ys, worst = C.check_batch(ttg, ts, 1e-8, ttg.precision.mixed, every=16)
-    assert worst <= 1e-10
-    # the oracle on every 128th TT: same ranks, and the distance to its
-    # result (device QR norms of the differences) within 1e-10
-    sel = range(0, 4096, 128)
-    refs = [O.round(ts[i], 1e-8) for i in sel]
+    # every status clean, ranks never above the input's, ||y - t|| <= eps ||t||
+    # on every 16th TT
+    ys, _ = C.check_batch(ttg, ts, 1e-8, ttg.precision[prec], every=16)
+    # The oracle on the same 256 TTs: equal ranks and ||y - y_oracle|| <=
+    # 1e-10 ||y_oracle||.  The distance to the input is not the measure: a
+    # bond whose smallest singular value lies below delta is truncated by the
+    # oracle too (TT 768, seed 1768: bond 2 keeps 63 of 64, ||y - t|| =
+    # 2.0e-9 ||t|| on both sides).
+    sel = list(range(0, 4096, 16))
+    _, refs = O.round_many_timed([ts[i] for i in sel], 1e-8, 0, 16)
+    refs = [r.cores() for r in refs]
     for i, ref in zip(sel, refs):
         assert O.ranks(ys[i]) == O.ranks(ref), i
     dn = C.diff_norms(ttg, [ys[i] for i in sel], refs, schedule=1)
