@@ -317,6 +317,37 @@ int32_t ttg_mlp_train_step(ttg_mlp* m, const float* x_dev, const float* t_dev, i
                            float lr, double* loss_host, void* stream);
 int64_t ttg_mlp_kernel_launches(const ttg_mlp* m);
 
+/* ---- several devices ---------------------------------------------------
+ * No counterpart in the reference, which rounds TTs and evaluates samples
+ * one after another on one core (round/tt_round.hpp:60-63,
+ * algebra/tt_eval.hpp:86-112).  Independent TTs and independent samples
+ * split across devices without any exchange step: each device runs the
+ * single-device entry point on its part from its own host thread, and the
+ * results land in the caller's host arrays in input order.
+ *
+ * ttg_shard_plan: the partition used by ttg_round_batch_devices.  TT i goes
+ * to part part_of[i] in [0, parts); cost[i] (optional) receives its
+ * estimated rounding cost, the algorithmic FLOP count F_round with the input
+ * ranks as output ranks.  Longest first, each TT to the least-loaded part
+ * (ties to the lower index): the result depends only on the shapes and
+ * `parts`, so every process computes the same partition.  Host code only;
+ * needs no device. */
+int32_t ttg_shard_plan(int32_t count, const ttg_tensor* ins, int32_t parts, int32_t* part_of,
+                       double* cost);
+/* ttg_round_batch with the TTs partitioned by ttg_shard_plan over the
+ * n_dev devices listed in devices[] (a device may appear more than once;
+ * its parts then run one after another).  Same options and results as
+ * ttg_round_batch, except that opts->bond_stats must be NULL.  On error no
+ * output is left allocated. */
+int32_t ttg_round_batch_devices(int32_t count, const ttg_tensor* ins,
+                                const ttg_round_options* opts, ttg_tensor* outs,
+                                ttg_round_result* results, int32_t n_dev, const int32_t* devices);
+/* ttg_eval_batch with the M multi-indices split into n_dev contiguous
+ * slices (sizes differing by at most one), slice p on devices[p]; the TT is
+ * copied to every device. */
+int32_t ttg_eval_batch_devices(const ttg_tensor* a, const int32_t* idx, int32_t M, double* out,
+                               int32_t n_dev, const int32_t* devices);
+
 /* ---- tensor-core GEMM ---------------------------------------------------
  * No counterpart in the reference (its GEMMs are Eigen products, e.g.
  * detail/contract.hpp:50).  C (M x N, row-major, ldc) = A (M x K) * B (K x N)
@@ -349,13 +380,19 @@ int32_t ttg_tc_gemm_f32(int32_t M, int32_t N, int32_t K, const float* A, int64_t
  * file-scope __device__ array of TTG_NOALLOC_SCRATCH_BYTES that every GPU
  * loading this library holds until the process exits.  A TT whose work copy
  * plus scratch exceeds that size, or with d > TTG_NOALLOC_MAX_D, is rejected
- * with TTG_ERR_NO_SPACE and a message in ttg_last_error().  The first call on
- * each device looks up the array's device address (cudaGetSymbolAddress) with
- * that device current; make that first call before any stream capture.  All
- * calls share the array and it keeps the last call's contents (every call
- * resets what must start at zero); calls that overlap on the GPU -- on
- * different streams or threads -- race on it and must be serialised by the
- * caller.  The call waits for its own stream to finish (it returns ranks). */
+ * with TTG_ERR_NO_SPACE and a message in ttg_last_error(); so is any core
+ * whose r*n, n*r' or r*n*r' alone exceeds the array.  The first call on each
+ * device looks up the array's device address (cudaGetSymbolAddress) with
+ * that device current, and so does the first call after a cudaDeviceReset
+ * (the address is cached per device and context); make that first call
+ * before any stream capture.  All calls share the array and it keeps the
+ * last call's contents (every call resets what must start at zero); calls
+ * that overlap on the GPU -- on different streams or threads -- race on it
+ * and must be serialised by the caller.  The call waits for its own stream
+ * to finish (it returns ranks).  Returns TTG_OK, or TTG_ERR_NOT_CONVERGED
+ * when a Jacobi SVD reached opts->max_sweeps (ttg_round reports this as
+ * round_result.converged = false): the rounded TT is written to out_dev and
+ * out_ranks in both cases. */
 #define TTG_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
 #define TTG_NOALLOC_MAX_D 256
 int32_t ttg_round_noalloc(int32_t d, const int32_t* ranks, const int32_t* modes,

@@ -179,6 +179,13 @@ def lib():
         "ttg_plan_schedule": (C.c_int32, [C.c_void_p]),
         "ttg_plan_graph": (C.c_int32, [C.c_void_p, C.c_int32]),
         "ttg_plan_autotune": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
+        "ttg_shard_plan": (C.c_int32, [C.c_int32, T, C.c_int32, C.POINTER(C.c_int32),
+                                       C.POINTER(C.c_double)]),
+        "ttg_round_batch_devices": (C.c_int32, [C.c_int32, T, O, T, R, C.c_int32,
+                                                C.POINTER(C.c_int32)]),
+        "ttg_eval_batch_devices": (C.c_int32, [T, C.POINTER(C.c_int32), C.c_int32,
+                                               C.POINTER(C.c_double), C.c_int32,
+                                               C.POINTER(C.c_int32)]),
         "ttg_tc_gemm_f32": (C.c_int32, [C.c_int32, C.c_int32, C.c_int32, C.c_void_p, C.c_int64,
                                         C.c_int64, C.c_void_p, C.c_int64, C.c_int64, C.c_void_p,
                                         C.c_int64, C.c_int32, C.c_void_p]),
@@ -292,15 +299,23 @@ def round(a, opts: RoundOptions | None = None, info: RoundResult | None = None):
     return _take(out)
 
 
-def round_batch(tts, opts: RoundOptions | None = None, results: list | None = None):
-    """Round many independent TTs in one persistent launch."""
+def round_batch(tts, opts: RoundOptions | None = None, results: list | None = None,
+                devices=None):
+    """Round many independent TTs in one persistent launch.  devices: a list
+    of CUDA device indices -- the batch is partitioned over them by
+    estimated rounding cost (shard_plan) and the results are returned in
+    input order."""
     srcs = [_In(t) for t in tts]
     n = len(srcs)
     ins = (_Tensor * max(n, 1))(*[s.t for s in srcs])
     outs = (_Tensor * max(n, 1))()
     res = (_Result * max(n, 1))()
     o = _opts(opts)
-    st = lib().ttg_round_batch(n, ins, C.byref(o), outs, res)
+    if devices is None:
+        st = lib().ttg_round_batch(n, ins, C.byref(o), outs, res)
+    else:
+        dv = (C.c_int32 * max(len(devices), 1))(*devices)
+        st = lib().ttg_round_batch_devices(n, ins, C.byref(o), outs, res, len(devices), dv)
     if st != 0:
         for i in range(n):
             if outs[i].owned:
@@ -375,15 +390,35 @@ def matmat(A, B):
     return _take(out)
 
 
-def eval_batch(a, idx):
-    """eval_batch (algebra/tt_eval.hpp:86-112); idx is (M, d) int."""
+def eval_batch(a, idx, devices=None):
+    """eval_batch (algebra/tt_eval.hpp:86-112); idx is (M, d) int.  devices:
+    a list of CUDA device indices over which the samples are split."""
     src = _In(a)
     idx = np.ascontiguousarray(idx, dtype=np.int32)
     M = idx.shape[0] if idx.ndim == 2 else 0
     out = np.zeros(max(M, 1), np.float64)
-    _check(lib().ttg_eval_batch(C.byref(src.t), idx.ctypes.data_as(C.POINTER(C.c_int32)), M,
-                                out.ctypes.data_as(C.POINTER(C.c_double))), "eval_batch")
+    ip, op = idx.ctypes.data_as(C.POINTER(C.c_int32)), out.ctypes.data_as(C.POINTER(C.c_double))
+    if devices is None:
+        _check(lib().ttg_eval_batch(C.byref(src.t), ip, M, op), "eval_batch")
+    else:
+        dv = (C.c_int32 * max(len(devices), 1))(*devices)
+        _check(lib().ttg_eval_batch_devices(C.byref(src.t), ip, M, op, len(devices), dv),
+               "eval_batch")
     return out[:M]
+
+
+def shard_plan(tts, parts):
+    """(part_of, cost): the partition of a batch over `parts` devices or
+    processes used by round_batch(devices=...) -- longest estimated rounding
+    cost first, each TT to the least-loaded part.  Host code; no device."""
+    srcs = [_In(t) for t in tts]
+    n = len(srcs)
+    ins = (_Tensor * max(n, 1))(*[s.t for s in srcs])
+    part_of = np.zeros(max(n, 1), np.int32)
+    cost = np.zeros(max(n, 1), np.float64)
+    _check(lib().ttg_shard_plan(n, ins, int(parts), part_of.ctypes.data_as(C.POINTER(C.c_int32)),
+                                cost.ctypes.data_as(C.POINTER(C.c_double))), "shard_plan")
+    return part_of[:n], cost[:n]
 
 
 def inner(a, b) -> float:

@@ -553,6 +553,14 @@ int32_t setup_wide(ttg_plan& P)
     const char* e = std::getenv("TTG_WIDE_TENSOR_CORES");
     j.tc = (j.mixed && e && e[0] == '1') ? 1 : 0;
   }
+  // Failure-path tests only (TTG_TEST_STALL_DEVICE_WAITS=1): no grid barrier
+  // completes and each wait gives up after ~1 ms, so that the call returns
+  // TTG_ERR_TIMEOUT through the same path a real stall would take.
+  {
+    const char* e = std::getenv("TTG_TEST_STALL_DEVICE_WAITS");
+    j.stall_waits = (e && e[0] == '1') ? 1 : 0;
+    j.wait_cycles = j.stall_waits ? 2000000ll : 4000000000ll;  // ~1 ms / ~2 s at 2 GHz
+  }
   j.tau = reinterpret_cast<double*>(b + otau);
   j.sig = reinterpret_cast<double*>(b + osig);
   j.sorted = reinterpret_cast<double*>(b + osorted);
@@ -983,39 +991,56 @@ int32_t first_bad_status(const ttg_plan& P)
   return TTG_OK;
 }
 
-cudaStream_t lib_stream()
+// State of the one-shot entry points, one set per device: the stream they
+// run on, the lock that serialises them, and the buffers they reuse
+// (grow-only, guarded by the lock), so repeated calls do not pay cudaMalloc /
+// cudaHostAlloc again.  Calls on different devices (the multi-device batch
+// entries run one host thread per device) proceed in parallel.
+constexpr int kMaxDevices = 64;
+
+struct DeviceState
 {
-  static cudaStream_t s = [] {
-    cudaStream_t x = nullptr;
-    cudaStreamCreateWithFlags(&x, cudaStreamNonBlocking);
-    return x;
-  }();
-  return s;
+  std::mutex mu;
+  std::once_flag stream_once;
+  cudaStream_t stream = nullptr;
+  DevMem dev_pool;
+  HostPinned host_pool;
+};
+
+DeviceState g_devices[kMaxDevices];
+
+DeviceState& dev_state()
+{
+  int dev = 0;
+  cudaGetDevice(&dev);
+  return g_devices[(dev >= 0 && dev < kMaxDevices) ? dev : 0];
 }
 
-std::mutex g_mu;
-
-// Buffers reused by the one-shot entry points (grow-only, guarded by g_mu),
-// so repeated calls do not pay cudaMalloc / cudaHostAlloc again.
-DevMem g_dev_pool;
-HostPinned g_host_pool;
+cudaStream_t lib_stream()
+{
+  DeviceState& s = dev_state();
+  std::call_once(s.stream_once,
+                 [&] { cudaStreamCreateWithFlags(&s.stream, cudaStreamNonBlocking); });
+  return s.stream;
+}
 
 struct PoolLease
 {
   ttg_plan& P;
-  explicit PoolLease(ttg_plan& p) : P(p)
+  DeviceState& S;
+  explicit PoolLease(ttg_plan& p) : P(p), S(dev_state())
   {
-    std::swap(P.dev.p, g_dev_pool.p);
-    std::swap(P.dev.bytes, g_dev_pool.bytes);
-    std::swap(P.host.p, g_host_pool.p);
-    std::swap(P.host.bytes, g_host_pool.bytes);
+    std::swap(P.dev.p, S.dev_pool.p);
+    std::swap(P.dev.bytes, S.dev_pool.bytes);
+    std::swap(P.host.p, S.host_pool.p);
+    std::swap(P.host.bytes, S.host_pool.bytes);
   }
   ~PoolLease()
   {
-    std::swap(P.dev.p, g_dev_pool.p);
-    std::swap(P.dev.bytes, g_dev_pool.bytes);
-    std::swap(P.host.p, g_host_pool.p);
-    std::swap(P.host.bytes, g_host_pool.bytes);
+    std::swap(P.dev.p, S.dev_pool.p);
+    std::swap(P.dev.bytes, S.dev_pool.bytes);
+    std::swap(P.host.p, S.host_pool.p);
+    std::swap(P.host.bytes, S.host_pool.bytes);
   }
 };
 
@@ -1409,7 +1434,7 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
   }
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_plan P;
   PoolLease lease(P);
   if (int32_t st = build_round_plan(P, count, ins, opts, op))
@@ -1470,7 +1495,7 @@ int32_t ttg_right_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   }
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_round_options o{};
   ttg_plan P;
   if (int32_t st = build_round_plan(P, 1, in, &o, "right_orthogonalize", kJobRightOrth))
@@ -1497,7 +1522,7 @@ int32_t ttg_left_orthogonalize(const ttg_tensor* in, ttg_tensor* out)
   }
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_round_options o{};
   ttg_plan P;
   if (int32_t st = build_round_plan(P, 1, in, &o, "left_orthogonalize", kJobLeftOrth))
@@ -1534,7 +1559,7 @@ int32_t ttg_soft_threshold(const ttg_tensor* in, double tau, ttg_tensor* out)
       return fail(TTG_ERR_SHAPE, "soft_threshold: dimension product exceeds INT_MAX");
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_round_options o{};
   o.eps = tau;
   o.precision = TTG_PREC_FP64;
@@ -1703,7 +1728,7 @@ static int32_t apply_round_common(const ttg_tensor* a, const ttg_tensor* x,
     }
     return TTG_OK;
   }
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_plan P;
   PoolLease lease(P);
   int32_t st = (mode == 2) ? build_stream_plan(P, A, X, opts)
@@ -1802,7 +1827,7 @@ int32_t ttg_frob_norm_apply(const ttg_tensor* a, const ttg_tensor* x, double* ou
       return fail(TTG_ERR_SHAPE, std::string(op) + ": m*n product exceeds INT_MAX");
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_plan P;
   PoolLease lease(P);
   if (int32_t st = build_apply_plan(P, A, X, false, nullptr))
@@ -1972,7 +1997,7 @@ int32_t ttg_eval_batch(const ttg_tensor* a, const int32_t* idx, int32_t M, doubl
     return fail(TTG_ERR_ARG, "eval_batch: null output");
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_plan P;
   if (int32_t st = build_eval_plan(P, a, idx, M))
     return st;
@@ -2009,7 +2034,7 @@ int32_t ttg_inner(const ttg_tensor* a, const ttg_tensor* b, double* out)
   }
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   ttg_plan P;
   P.shapes = {A, B};
   add_tensor(P, A, true, nullptr);
@@ -2051,7 +2076,7 @@ int32_t ttg_device_fp64_peak(double* tflops)
     return fail(TTG_ERR_ARG, "fp64_peak: null output");
   if (int32_t st = need_device())
     return st;
-  std::lock_guard<std::mutex> lk(g_mu);
+  std::lock_guard<std::mutex> lk(dev_state().mu);
   const int grid = 4 * std::max(device().sms, 1), block = 256, iters = 1 << 14;
   DevMem buf;
   TTG_CUDA(buf.ensure(sizeof(double) * static_cast<size_t>(grid) * block));

@@ -86,3 +86,60 @@ def test_clock_sample_parsing():
     c.lines = ["0, 1100, 2070, 500.0, Active, Active, Not Active, Not Active, Not Active"]
     s = c.summary()
     assert s["reasons"] == ["hw_slowdown"] and not bench.clocks_ok(s)
+
+
+def _shard_worker(rank, world, port, q):
+    # Each rank rounds its part of one batch with the oracle (the CPU worker
+    # of this test); rank 0 gathers through host memory (gloo).
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    from oracle import pyoracle as O
+    from tensor_train_gb300 import shard
+    tts = [O.random_uneven(1000 + i, 8, 12, 4, 16) for i in range(24)]
+    mine = shard.my_part(tts, rank, world)
+    ys = shard.round_batch_distributed(tts, worker=lambda part: [O.round(t, 1e-8) for t in part])
+    dist.destroy_process_group()
+    q.put((rank, mine, ys))
+
+
+def test_two_gloo_ranks_round_one_batch():
+    import numpy as np
+    from oracle import pyoracle as O
+    ctx = mp.get_context("spawn")
+    q = ctx.Queue()
+    port = _free_port()
+    procs = [ctx.Process(target=_shard_worker, args=(r, 2, port, q)) for r in range(2)]
+    for p in procs:
+        p.start()
+    out = sorted((q.get(timeout=300) for _ in procs), key=lambda x: x[0])
+    for p in procs:
+        p.join(timeout=60)
+        assert p.exitcode == 0
+    (_, mine0, ys0), (_, mine1, ys1) = out
+    assert ys1 is None and ys0 is not None
+    # the parts cover the batch once, and both ranks did work
+    assert sorted(mine0 + mine1) == list(range(24)) and mine0 and mine1
+    # the gathered result equals the single-rank result bit for bit, in order
+    tts = [O.random_uneven(1000 + i, 8, 12, 4, 16) for i in range(24)]
+    single = [O.round(t, 1e-8) for t in tts]
+    for a, b in zip(ys0, single):
+        assert len(a) == len(b) and all(np.array_equal(x, y) for x, y in zip(a, b))
+
+
+def test_shard_plan_balances_by_cost(ttg):
+    # Longest estimated cost first to the least-loaded part: deterministic,
+    # every TT placed once, loads within the largest single cost.
+    import numpy as np
+    from oracle import pyoracle as O
+    from tensor_train_gb300.flops import round_flops
+    tts = [O.random_uneven(1000 + i) for i in range(64)]
+    part_of, cost = ttg.shard_plan(tts, 3)
+    assert np.array_equal(part_of, ttg.shard_plan(tts, 3)[0])
+    assert set(part_of.tolist()) == {0, 1, 2}
+    for t, c in zip(tts, cost):
+        modes = [x.shape[1] for x in t]
+        r = [t[0].shape[0]] + [x.shape[-1] for x in t]
+        assert abs(c - round_flops(modes, r, r)) <= 1e-9 * c
+    loads = [cost[part_of == p].sum() for p in range(3)]
+    assert max(loads) - min(loads) <= cost.max()
+    assert np.array_equal(ttg.shard_plan(tts, 1)[0], np.zeros(64, np.int32))
