@@ -17,6 +17,7 @@
 #include <mutex>
 #include <string>
 
+#include <cuda.h>
 #include <cuda_runtime.h>
 
 #include "../../include/ttg.h"
@@ -112,6 +113,7 @@ __global__ void noalloc_pack(const double* arena, const CoreSlot* slots, const T
 
 std::mutex g_noalloc_mu;
 unsigned char* g_noalloc_ptr[kMaxDevices] = {};
+unsigned long long g_noalloc_ctx[kMaxDevices] = {};
 
 int32_t nfail(int32_t st, const std::string& msg)
 {
@@ -119,8 +121,44 @@ int32_t nfail(int32_t st, const std::string& msg)
   return st;
 }
 
+using CtxGetCurrentFn = CUresult (*)(CUcontext*);
+using CtxGetIdFn = CUresult (*)(CUcontext, unsigned long long*);
+
+// Unique id of the context current on this thread (0 if the driver cannot
+// tell).  A cudaDeviceReset ends the device's primary context; the next
+// runtime call makes a new one with a new id, in which the array has a new
+// address.  The driver functions are fetched through the runtime, so the
+// library does not link libcuda itself.
+unsigned long long current_context_id()
+{
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    void* f = nullptr;
+    cudaDriverEntryPointQueryResult q{};
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_current = reinterpret_cast<CtxGetCurrentFn>(f);
+    f = nullptr;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetId", &f, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      get_id = reinterpret_cast<CtxGetIdFn>(f);
+  });
+  CUcontext ctx = nullptr;
+  unsigned long long id = 0;
+  if (get_current && get_id && get_current(&ctx) == CUDA_SUCCESS && ctx &&
+      get_id(ctx, &id) == CUDA_SUCCESS)
+    return id;
+  return 0;
+}
+
 // Device address of the scratch array for the current device.  Looked up
-// once per device (with that device current) and cached.
+// with that device current on the first call in each context of the device
+// (the first call on the device, and the first after a cudaDeviceReset) and
+// cached; later calls reuse the cached address.
 int32_t scratch_for_device(unsigned char** out)
 {
   int dev = 0;
@@ -129,8 +167,15 @@ int32_t scratch_for_device(unsigned char** out)
     return nfail(TTG_ERR_CUDA, std::string("round_noalloc: cudaGetDevice: ") + cudaGetErrorString(e));
   if (dev < 0 || dev >= kMaxDevices)
     return nfail(TTG_ERR_NO_SPACE, "round_noalloc: device index above 63");
+  // cudaSetDevice makes the device's primary context current on this thread
+  // (cudaGetDevice alone does not), so the context id read next is the one
+  // the kernels of this call will run in.
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess)
+    return nfail(TTG_ERR_CUDA, std::string("round_noalloc: cudaSetDevice: ") + cudaGetErrorString(e));
+  const unsigned long long ctx = current_context_id();
   std::lock_guard<std::mutex> lk(g_noalloc_mu);
-  if (!g_noalloc_ptr[dev])
+  if (!g_noalloc_ptr[dev] || ctx != g_noalloc_ctx[dev])
   {
     void* p = nullptr;
     e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
@@ -138,6 +183,9 @@ int32_t scratch_for_device(unsigned char** out)
       return nfail(TTG_ERR_CUDA, std::string("round_noalloc: cudaGetSymbolAddress: ") +
                                      cudaGetErrorString(e));
     g_noalloc_ptr[dev] = static_cast<unsigned char*>(p);
+    // Looked up after the symbol so that a context made by the lookup
+    // itself is the one recorded.
+    g_noalloc_ctx[dev] = current_context_id();
   }
   *out = g_noalloc_ptr[dev];
   return TTG_OK;
@@ -215,12 +263,24 @@ int32_t ttg_round_noalloc(int32_t d, const int32_t* ranks, const int32_t* modes,
   }
   if (d > 0 && (ranks[0] != 1 || ranks[d] != 1))
     return nfail(TTG_ERR_SHAPE, "round_noalloc: tt: r_0 and r_d must be 1");
+  // Sizes are bounded before any of them is multiplied further: no factor
+  // of a core (r*n, n*r', r*n*r') and no running total may exceed the
+  // doubles the array holds, so every later product of two such terms
+  // stays far inside int64.
+  constexpr int64_t kCapDoubles = static_cast<int64_t>(kNoallocScratchBytes / sizeof(double));
   for (int k = 0; k < d; ++k)
   {
     if (modes[k] <= 0)
       return nfail(TTG_ERR_SHAPE, "round_noalloc: tt_core: dimensions must be positive");
     s.modes[k] = modes[k];
-    total += static_cast<int64_t>(ranks[k]) * modes[k] * ranks[k + 1];
+    const int64_t rn = static_cast<int64_t>(ranks[k]) * modes[k];
+    const int64_t nrp = static_cast<int64_t>(modes[k]) * ranks[k + 1];
+    if (rn > kCapDoubles || nrp > kCapDoubles || rn * ranks[k + 1] > kCapDoubles ||
+        total + rn * ranks[k + 1] > kCapDoubles)
+      return nfail(TTG_ERR_NO_SPACE,
+                   "round_noalloc: core " + std::to_string(k) + " does not fit the fixed scratch of " +
+                       std::to_string(kNoallocScratchBytes) + " bytes (use ttg_round instead)");
+    total += rn * ranks[k + 1];
   }
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (d <= 1)
@@ -304,7 +364,13 @@ int32_t ttg_round_noalloc(int32_t d, const int32_t* ranks, const int32_t* modes,
   for (int k = 0; k <= d; ++k)
     out_ranks[k] = host_result[k];
   const int32_t status = host_result[d + 1];
-  if (status != TTG_OK && status != TTG_ERR_NOT_CONVERGED)
+  if (status == TTG_ERR_NOT_CONVERGED)
+    // The result is complete (out_dev and out_ranks are written); Jacobi hit
+    // its sweep limit on at least one bond, which ttg_round reports through
+    // round_result.converged = false.
+    return nfail(status, "round_noalloc: a Jacobi SVD reached max_sweeps before converging; the "
+                         "rounded TT was written");
+  if (status != TTG_OK)
     return nfail(status, std::string("round_noalloc: device status ") + ttg_status_string(status));
   return TTG_OK;
 }

@@ -34,7 +34,9 @@ def _bind(ttg):
     return f
 
 
-def _noalloc_round(ttg, cores, opts):
+def _call(ttg, cores, opts, in_place=False):
+    """One ttg_round_noalloc call on device copies of `cores`; returns
+    (status, output cores).  in_place: the output buffer is the input's."""
     import torch
     f = _bind(ttg)
     d = len(cores)
@@ -42,7 +44,7 @@ def _noalloc_round(ttg, cores, opts):
     modes = np.array([c.shape[1] for c in cores], np.int32)
     flat = np.concatenate([c.ravel() for c in cores])
     src = torch.from_numpy(flat).to("cuda")
-    dst = torch.full_like(src, float("nan"))
+    dst = src if in_place else torch.full_like(src, float("nan"))
     out_ranks = np.zeros(d + 1, np.int32)
     o = ttg._opts(opts)
     stream = torch.cuda.current_stream().cuda_stream
@@ -50,8 +52,6 @@ def _noalloc_round(ttg, cores, opts):
            modes.ctypes.data_as(C.POINTER(C.c_int32)), C.c_void_p(src.data_ptr()),
            C.c_void_p(dst.data_ptr()), out_ranks.ctypes.data_as(C.POINTER(C.c_int32)),
            C.byref(o), C.c_void_p(stream))
-    if st != 0:
-        raise ttg.TTGError(st, ttg.lib().ttg_last_error().decode())
     out = dst.cpu().numpy()
     res, off = [], 0
     for k in range(d):
@@ -59,6 +59,13 @@ def _noalloc_round(ttg, cores, opts):
         n = int(np.prod(shp))
         res.append(out[off:off + n].reshape(shp).copy())
         off += n
+    return st, res
+
+
+def _noalloc_round(ttg, cores, opts, in_place=False):
+    st, res = _call(ttg, cores, opts, in_place)
+    if st != 0:
+        raise ttg.TTGError(st, ttg.lib().ttg_last_error().decode())
     return res
 
 
@@ -97,3 +104,37 @@ def test_noalloc_rejects_oversize(ttg):
            out_ranks.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(o), None)
     assert st == 11
     assert b"scratch" in ttg.lib().ttg_last_error()
+
+
+def test_noalloc_edge_cases(ttg):
+    # d = 1 (returned unchanged by a device-to-device copy), a max_rank cap,
+    # and a call whose output buffer is its input buffer (the input is copied
+    # into the fixed array before the sweep writes anything).
+    one = [O.random([5], 1, 3)[0]]
+    y = _noalloc_round(ttg, one, ttg.RoundOptions(eps=1e-8))
+    assert O.ranks(y) == [1, 1] and np.array_equal(y[0], one[0])
+    t1, _ = _inputs()
+    for opts in (ttg.RoundOptions(eps=1e-8, max_rank=2), ttg.RoundOptions(eps=1e-8)):
+        ref = ttg.round(t1, opts)
+        for in_place in (False, True):
+            y = _noalloc_round(ttg, t1, opts, in_place=in_place)
+            assert O.ranks(y) == O.ranks(ref), (O.ranks(y), O.ranks(ref))
+            assert O.rel_err(y, ref) <= TOL
+
+
+def test_noalloc_reports_non_convergence(ttg):
+    # One Jacobi sweep on rank-64 bonds cannot converge: the call says so
+    # (TTG_ERR_NOT_CONVERGED, as ttg_round's converged = false) and still
+    # writes the rounded TT.
+    t = O.random([4] * 8, 64, 11, fan_in_scale=True)
+    opts = ttg.RoundOptions(eps=1e-8, max_sweeps=1)
+    info = ttg.RoundResult()
+    ttg.round(t, opts, info)
+    assert not info.converged
+    st, y = _call(ttg, t, opts)
+    assert st == 6, st
+    assert b"max_sweeps" in ttg.lib().ttg_last_error()
+    assert O.ranks(y)[0] == 1 and all(np.isfinite(c).all() for c in y)
+    # the default sweep limit converges on the same input
+    y = _noalloc_round(ttg, t, ttg.RoundOptions(eps=1e-8))
+    assert O.rel_err(y, O.round(t, 1e-8)) <= TOL
