@@ -144,6 +144,8 @@ struct WideJob
   int mixed;           // 1: FP32 + df64 SVD sweeps
   int tc;              // 1: contractions with K <= 512 on the tensor cores (sliced BF16)
   int kind;            // kJobRound or kJobStreamMatvec / kJobStreamMatmat
+  int stall_waits;     // failure-path tests only: no grid barrier completes
+  long long wait_cycles;  // limit of one grid-barrier wait (clock cycles)
   const int* a_idx;    // streaming: operand and output TT of each item
   const int* b_idx;
   const int* out_idx;

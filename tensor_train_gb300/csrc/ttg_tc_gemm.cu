@@ -19,6 +19,7 @@
 // the failure in *err, waits (bounded) once more for the MMAs in flight,
 // frees its TMEM and returns.
 #include <cstdint>
+#include <cstdlib>
 #include <cstring>
 #include <mutex>
 #include <string>
@@ -38,6 +39,8 @@ namespace
 constexpr int kBM = 128, kBK = 64, kTcThreads = 128;
 // ~2 s at 2 GHz: far beyond any MMA group's latency.
 constexpr long long kWaitCycles = 4000000000ll;
+// ~1 ms: the stalled wait of the failure-path tests.
+constexpr long long kStallWaitCycles = 2000000ll;
 
 struct TcGemmArgs
 {
@@ -51,13 +54,17 @@ struct TcGemmArgs
   const float* bias;
   int relu, accumulate, splits;
   int* err;
+  // Failure-path tests only: before each MMA completion wait, wait on an
+  // mbarrier nothing arrives on, so that the wait runs out (~1 ms) and the
+  // kernel takes its timeout path.
+  int stall_waits;
 };
 
-__device__ bool wait_bounded(uint64_t* mbar, uint32_t parity)
+__device__ bool wait_bounded(uint64_t* mbar, uint32_t parity, long long limit = kWaitCycles)
 {
   const long long t0 = clock64();
   while (!tc::mbar_wait(mbar, parity, 64))
-    if (clock64() - t0 > kWaitCycles)
+    if (clock64() - t0 > limit)
       return false;
   return true;
 }
@@ -80,6 +87,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_gemm_kernel(TcGemmArgs g)
   uint8_t* b_hi = a_lo + kTileA;
   uint8_t* b_lo = b_hi + kTileB;
   __shared__ __align__(8) uint64_t mbar;
+  __shared__ __align__(8) uint64_t stall_mbar;  // never arrived on
   __shared__ uint32_t tmem_base;
   __shared__ int failed;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -90,6 +98,7 @@ __global__ void __launch_bounds__(kTcThreads) tc_gemm_kernel(TcGemmArgs g)
   if (threadIdx.x == 0)
   {
     tc::mbar_init(&mbar, 1);
+    tc::mbar_init(&stall_mbar, 1);
     failed = 0;
   }
   tc::fence_before_sync();
@@ -146,7 +155,9 @@ __global__ void __launch_bounds__(kTcThreads) tc_gemm_kernel(TcGemmArgs g)
     }
     issued = true;
     // The next chunk overwrites the operands: wait for these MMAs.
-    if (!wait_bounded(&mbar, phase))
+    bool done = !g.stall_waits || wait_bounded(&stall_mbar, 0, kStallWaitCycles);
+    done = done && wait_bounded(&mbar, phase);
+    if (!done)
     {
       if (lane == 0)
         atomicExch(&failed, 1);
@@ -269,8 +280,10 @@ cudaError_t tc_gemm_f32(cudaStream_t st, int M, int N, int K, const float* A, in
   int* err = error_flag();
   if (!err)
     return cudaErrorMemoryAllocation;
+  const char* stall = std::getenv("TTG_TEST_STALL_DEVICE_WAITS");
   TcGemmArgs g{M, N, K, A, a_rs, a_cs, B, b_rs, b_cs, C, ldc, bias,
-               relu ? 1 : 0, accumulate ? 1 : 0, splits, err};
+               relu ? 1 : 0, accumulate ? 1 : 0, splits, err,
+               (stall && stall[0] == '1') ? 1 : 0};
   if (N > 64)
     return launch_bn<128>(g, st);
   if (N > 32)

@@ -22,7 +22,7 @@
 // df64 sweeps (FP32 pipes) polish to FP64-level accuracy, as in the
 // one-CTA-per-TT kernel.
 //
-// Every barrier wait is bounded (kGridWaitCycles): a CTA that gives up sets
+// Every barrier wait is bounded (WideJob::wait_cycles, ~2 s by default): a CTA that gives up sets
 // the shared error word, every other CTA sees it at its next barrier, and
 // the kernel returns; the host reports TTG_ERR_TIMEOUT.
 #include <cfloat>
@@ -40,12 +40,11 @@
 namespace ttg
 {
 
-constexpr long long kGridWaitCycles = 4000000000ll;  // ~2 s at 2 GHz
-
 // Bounded barrier of the `count` CTAs of a team (the whole grid, or a group
 // of it), by generation counter.  All CTAs are co-resident (cooperative
-// launch).  Returns false once any CTA of the team timed out.
-__device__ bool grid_sync(GridBar* gb, unsigned int count)
+// launch).  Returns false once any CTA of the team timed out (after
+// `limit` clock cycles of waiting).
+__device__ bool grid_sync(GridBar* gb, unsigned int count, long long limit)
 {
   __shared__ int ok_sh;
   __syncthreads();
@@ -69,7 +68,7 @@ __device__ bool grid_sync(GridBar* gb, unsigned int count)
       {
         if (*errp)
           break;
-        if (clock64() - t0 > kGridWaitCycles)
+        if (clock64() - t0 > limit)
         {
           atomicExch(&gb->err, 1);
           break;
@@ -86,10 +85,18 @@ __device__ bool grid_sync(GridBar* gb, unsigned int count)
   return ok_sh != 0;
 }
 
+// The team's barrier.  job.stall_waits (set only by the failure-path tests)
+// counts one CTA more than the team holds, so that no barrier ever
+// completes and every wait runs out after job.wait_cycles.
+__device__ bool grid_sync(const WideJob& job)
+{
+  return grid_sync(job.bar, job.size + (job.stall_waits ? 1u : 0u), job.wait_cycles);
+}
+
 #define WSYNC()                 \
   do                            \
   {                             \
-    if (!grid_sync(job.bar, job.size)) \
+    if (!grid_sync(job)) \
       return false;             \
   } while (0)
 
@@ -207,7 +214,7 @@ __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, Ct
     reflect(0);
   for (int j = 0; j < k; ++j)
   {
-    if (!grid_sync(job.bar, job.size))
+    if (!grid_sync(job))
     {
       *ok = false;
       return k;
@@ -237,7 +244,7 @@ __device__ int wide_qr(const WideJob& job, View X, int h, int c, WideSmem sm, Ct
     for (int i = threadIdx.x; i < k; i += blockDim.x)
       job.R[i + static_cast<int64_t>(l) * k] = (i <= l) ? y[i] : 0.0;
   }
-  if (!grid_sync(job.bar, job.size))
+  if (!grid_sync(job))
     *ok = false;
   return k;
 }
@@ -784,7 +791,7 @@ __device__ int wide_norm_step(const WideJob& job, TTInfo& T, CoreSlot* S, int d,
   {
     if (job.rank == 0)
       zero_tt(job.arena, S, d);
-    return grid_sync(job.bar, job.size) ? 1 : -1;
+    return grid_sync(job) ? 1 : -1;
   }
   *delta = job.eps * nrm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
   if (lead)
