@@ -471,6 +471,135 @@ __device__ __noinline__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, in
 }
 
 // ---------------------------------------------------------------------------
+// No-truncation certificate of a truncated-SVD step.
+//
+// svd_step keeps all c singular values of a bond exactly when the smallest
+// one alone exceeds the tail budget: sigma_c^2 > delta^2 (tail rule of
+// truncate_eps_rank, types/tt_eigen_bridge.hpp:172-197, with no max_rank
+// cap below c).  Then the SVD only rotates a basis: U diag(s) V^T = Q R gives
+// the same represented tensor and the same rank whether the left factor is U
+// and diag(s) V^T is absorbed, or Q and R.  This routine proves that case
+// from the R factor of the step's QR, so the Jacobi SVD can be skipped.
+//
+// Test: R^T R - tau I is positive definite, shown by an LDL^T elimination
+// that meets only positive pivots.  tau covers every rounding error between
+// the bond matrix X and the computed pivots:
+//   * sigma_min(X) >= sigma_min(R) - e_R with e_R = c h u ||R||_F, a bound on
+//     the backward error of the Householder QR that produced R (Higham,
+//     Accuracy and Stability of Numerical Algorithms, 2nd ed., thm. 19.4,
+//     with the constant taken generously);
+//   * forming R^T R and eliminating it perturb its eigenvalues by at most
+//     2 (c + 1)^2 u ||R||_F^2 (thms. 3.5 and 10.3 there, normwise);
+// so positive pivots with tau = (delta + e_R)^2 + 2 (c + 1)^2 u ||R||_F^2
+// imply sigma_min(X) > delta.  u is the unit roundoff of the arithmetic
+// (2^-53 for FP64; 2^-47 for df64, below its 48-bit significand).  A NaN
+// anywhere fails the test (the comparison with a NaN pivot is false), and
+// the caller then runs the SVD, which reports it.
+//
+// R: c x c upper triangular, column-major (ld c).  G: c x c scratch of
+// E-sized elements (lower triangle used).  h: rows of the step's matrix.
+// ---------------------------------------------------------------------------
+template <class E>
+struct CertOps;
+template <>
+struct CertOps<double>
+{
+  static __device__ __forceinline__ double from(double x) { return x; }
+  static __device__ __forceinline__ double to(double x) { return x; }
+  static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
+  static __device__ __forceinline__ double neg(double a) { return -a; }
+  static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static constexpr double u = 1.1102230246251565e-16;  // 2^-53
+};
+template <>
+struct CertOps<df64>
+{
+  static __device__ __forceinline__ df64 from(double x) { return df_from(x); }
+  static __device__ __forceinline__ double to(df64 x) { return df_to(x); }
+  static __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return df_fma(a, b, c); }
+  static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
+  static __device__ __forceinline__ df64 neg(df64 a) { return df_neg(a); }
+  static __device__ __forceinline__ df64 sub(df64 a, df64 b) { return df_sub(a, b); }
+  static constexpr double u = 7.105427357601002e-15;  // 2^-47
+};
+
+template <class E>
+__device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, int h, double delta,
+                                                       E* G, CtaShared& sh)
+{
+  using O = CertOps<E>;
+  if (c < 1)
+    return false;
+  // Scale by a power of two (exact) so that max |R| is ~1: keeps the
+  // squares inside the FP32 exponent range of df64.
+  const double s = cta_pow2_of_max(View{R, 1, c}, c, c, sh);
+  const double is = 1.0 / s;
+  const int64_t cc = static_cast<int64_t>(c) * c;
+  double part = 0.0;
+  for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+  {
+    const double x = R[t] * is;
+    part += x * x;
+  }
+  const double fro2 = cta_sum(part, sh);  // ||R / s||_F^2
+  if (!(fro2 > 0.0) || !isfinite(fro2))
+    return false;
+  const double dl = delta * is;
+  const double eR = static_cast<double>(c) * h * O::u * sqrt(fro2);
+  const double tau = (dl + eR) * (dl + eR) + 2.0 * (c + 1.0) * (c + 1.0) * O::u * fro2;
+  // G = (R/s)^T (R/s) - tau I, lower triangle: G(i, j) = sum_{p <= j} R(p, i) R(p, j).
+  const int64_t ntri = static_cast<int64_t>(c) * (c + 1) / 2;
+  for (int64_t t = threadIdx.x; t < ntri; t += blockDim.x)
+  {
+    // t -> (i, j), i >= j, packed by rows of the lower triangle.
+    int i = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+    while (static_cast<int64_t>(i) * (i + 1) / 2 > t)
+      --i;
+    while (static_cast<int64_t>(i + 1) * (i + 2) / 2 <= t)
+      ++i;
+    const int j = static_cast<int>(t - static_cast<int64_t>(i) * (i + 1) / 2);
+    const double* ri = R + static_cast<int64_t>(i) * c;
+    const double* rj = R + static_cast<int64_t>(j) * c;
+    E acc = O::from(0.0);
+    for (int p = 0; p <= j; ++p)
+      acc = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), acc);
+    if (i == j)
+      acc = O::sub(acc, O::from(tau));
+    G[i + static_cast<int64_t>(j) * c] = acc;
+  }
+  __syncthreads();
+  // LDL^T elimination of the lower triangle (the pivots are all that is
+  // needed): G(i, k) -= G(i, j) G(k, j) / G(j, j) for j < k <= i.
+  for (int j = 0; j < c; ++j)
+  {
+    const double piv = O::to(G[j + static_cast<int64_t>(j) * c]);
+    if (!(piv > 0.0))
+      return false;  // every thread reads the same pivot: a uniform exit
+    if (j == c - 1)
+      break;
+    const E inv = O::from(1.0 / piv);
+    const int rem = c - 1 - j;  // trailing order
+    const int64_t ntr = static_cast<int64_t>(rem) * (rem + 1) / 2;
+    const E* gj = G + static_cast<int64_t>(j) * c;
+    for (int64_t t = threadIdx.x; t < ntr; t += blockDim.x)
+    {
+      int a = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+      while (static_cast<int64_t>(a) * (a + 1) / 2 > t)
+        --a;
+      while (static_cast<int64_t>(a + 1) * (a + 2) / 2 <= t)
+        ++a;
+      const int b = static_cast<int>(t - static_cast<int64_t>(a) * (a + 1) / 2);
+      const int i = j + 1 + a, k = j + 1 + b;  // i >= k > j
+      E& g = G[i + static_cast<int64_t>(k) * c];
+      g = O::fma(O::neg(O::mul(gj[i], inv)), gj[k], g);
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// ---------------------------------------------------------------------------
 // Mixed-precision one-sided Jacobi: the sweeps that do most of the rotating
 // run in FP32, a df64 refinement restores FP64-level accuracy.
 //   1. FP32 copy of src (m x n, m >= n) and V32 = I in fbuf

@@ -113,7 +113,12 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
   // they always land in the truncated tail: Jacobi does not rotate them.
   const int nsv = h < c ? h : c;
   const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
-  if (h >= 2 * c)
+  // No-truncation certificate (cta_certify_no_truncation): tried whenever no
+  // singular value is asked for and max_rank cannot cut below c; for h >= c
+  // the step then takes the QR route of the h >= 2c branch below.
+  const bool certify = bs == nullptr && s_out == nullptr && h >= c && c >= 2 &&
+                       (max_rank <= 0 || max_rank >= c);
+  if (h >= 2 * c || certify)
   {
     double* W = bump.take(static_cast<int64_t>(h) * c);
     double* tau = bump.take(c);
@@ -154,36 +159,55 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       cta_householder_qr(W, h, c, h, tau, sh);
       cta_extract_r(R, W, c, c, h);
     }
-    if (mixed)
+    const bool certified =
+      certify && (mixed ? cta_certify_no_truncation<df64>(R, c, h, delta, reinterpret_cast<df64*>(A), sh)
+                        : cta_certify_no_truncation<double>(R, c, h, delta, A, sh));
+    int r_new = c;
+    if (certified)
     {
-      float* fbuf = A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(cc));
-      double* tmp = bump.take(3 * cc);
-      sweeps = cta_jacobi_mixed(View{R, 1, c}, c, c, A, c, nullptr, max_sweeps, &conv, nrm, fbuf,
-                                tmp, sh, GemmDf{}, floor2);
+      // sigma_min > delta: every singular value is kept, U = Q, F = R.
+      for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+      {
+        const int i = static_cast<int>(t % c), jj = static_cast<int>(t / c);
+        Uc[t] = i == jj ? 1.0 : 0.0;
+        F[static_cast<int64_t>(i) * c + jj] = R[t];
+      }
+      __syncthreads();
     }
     else
     {
-      for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
-        A[t] = R[t];
+      if (mixed)
+      {
+        float* fbuf =
+          A_in_smem ? reinterpret_cast<float*>(A) : reinterpret_cast<float*>(bump.take(cc));
+        double* tmp = bump.take(3 * cc);
+        sweeps = cta_jacobi_mixed(View{R, 1, c}, c, c, A, c, nullptr, max_sweeps, &conv, nrm,
+                                  fbuf, tmp, sh, GemmDf{}, floor2);
+      }
+      else
+      {
+        for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+          A[t] = R[t];
+        __syncthreads();
+        sweeps = cta_jacobi<double>(A, c, c, c, nullptr, 0, max_sweeps, &conv, nrm, sh, floor2,
+                                    kJacobiStopRel);
+      }
+      cta_col_norms(A, c, c, c, sig);
+      cta_argsort_desc(sig, c, ord, sorted);
+      if (threadIdx.x == 0)
+        sh.ival[0] = trunc_rank_serial(sorted, c, delta, max_rank);
       __syncthreads();
-      sweeps = cta_jacobi<double>(A, c, c, c, nullptr, 0, max_sweeps, &conv, nrm, sh, floor2,
-                                  kJacobiStopRel);
+      r_new = sh.ival[0];
+      for (int64_t t = threadIdx.x; t < static_cast<int64_t>(c) * r_new; t += blockDim.x)
+      {
+        const int i = static_cast<int>(t % c), jj = static_cast<int>(t / c);
+        const double s = sorted[jj];
+        Uc[t] = s > 0.0 ? A[i + static_cast<int64_t>(ord[jj]) * c] / s : 0.0;
+      }
+      __syncthreads();
+      // F = Uc^T R  (= diag(s) V^T restricted to the kept rows).
+      gemm_sel(mixed, r_new, c, c, View{Uc, c, 1}, View{R, 1, c}, F, c, 1, sh);
     }
-    cta_col_norms(A, c, c, c, sig);
-    cta_argsort_desc(sig, c, ord, sorted);
-    if (threadIdx.x == 0)
-      sh.ival[0] = trunc_rank_serial(sorted, c, delta, max_rank);
-    __syncthreads();
-    const int r_new = sh.ival[0];
-    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(c) * r_new; t += blockDim.x)
-    {
-      const int i = static_cast<int>(t % c), jj = static_cast<int>(t / c);
-      const double s = sorted[jj];
-      Uc[t] = s > 0.0 ? A[i + static_cast<int64_t>(ord[jj]) * c] / s : 0.0;
-    }
-    __syncthreads();
-    // F = Uc^T R  (= diag(s) V^T restricted to the kept rows).
-    gemm_sel(mixed, r_new, c, c, View{Uc, c, 1}, View{R, 1, c}, F, c, 1, sh);
     // U = Q [Uc; 0] by applying the reflectors.
     if (mixed)
     {
@@ -212,10 +236,11 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       __syncthreads();
       cta_apply_q(W, h, c, h, tau, U, r_new, h);
     }
-    record_bond(bs, sorted, c, r_new);
+    if (!certified)
+      record_bond(bs, sorted, c, r_new);
     if (threadIdx.x == 0)
     {
-      if (!finite(sorted[0]))
+      if (!certified && !finite(sorted[0]))
         set_status(T, kStatusNan);
       if (!conv)
         set_status(T, kStatusNotConverged);
@@ -1046,6 +1071,297 @@ __device__ __noinline__ void stream_tt(const RoundJob& job, int item, double* sc
 
 // MinBlocks CTAs of 256 threads resident per SM (the register cap follows:
 // 128, 85 or 64 per thread); the autotuner picks the instantiation.
+// ---------------------------------------------------------------------------
+// ALS and two-site DMRG rounding (round/tt_als.hpp:52-206,
+// round/tt_dmrg.hpp:45-212), one CTA per (Y, X) pair: Y = TT a_idx[i] is the
+// tensor to compress, X = TT b_idx[i] the start TT, overwritten in its slots
+// (bond capacities fixed by the host).  The left and right environments,
+// the bond spectra of two consecutive sweep pairs and the bond capacities
+// live in the pair's region of the arena (TTInfo::env_off of X):
+//   L[k] at env + k*es, R[k] at env + (d+1+k)*es (k = 0..d), then cmax,
+//   s_prev / s_now ((d-1) bonds x cmax each), their counts and the bond
+//   capacities cap[0..d], as doubles (written by the host).
+// All arithmetic is FP64.
+// ---------------------------------------------------------------------------
+
+// contract_inner_step (detail/contract.hpp:155-205):
+// out (rap x rbp) = sum_{a,b,i} E(a, b) ca(a, i, a') cb(b, i, b').
+__device__ void env_left(const double* E, const double* ca, int ra, int n, int rap,
+                         const double* cb, int rb, int rbp, double* out, Bump bump, CtaShared& sh)
+{
+  const int64_t w = static_cast<int64_t>(n) * rap;
+  double* tmp = bump.take(static_cast<int64_t>(rb) * w);
+  cta_gemm(rb, static_cast<int>(w), ra, View{E, 1, rb}, View{ca, w, 1}, tmp, w, 1, sh);
+  cta_gemm(rap, rbp, rb * n, View{tmp, 1, rap}, View{cb, rbp, 1}, out, rbp, 1, sh);
+}
+
+// contract_inner_step_right (detail/contract.hpp:90-139):
+// out (ra x rb) = sum_{i,a',b'} ca(a, i, a') F(a', b') cb(b, i, b').
+__device__ void env_right(const double* ca, int ra, int n, int rap, const double* cb, int rb,
+                          int rbp, const double* F, double* out, Bump bump, CtaShared& sh)
+{
+  const int64_t w = static_cast<int64_t>(n) * rbp;
+  double* T1 = bump.take(static_cast<int64_t>(ra) * w);
+  cta_gemm(ra * n, rbp, rap, View{ca, rap, 1}, View{F, rbp, 1}, T1, rbp, 1, sh);
+  cta_gemm(ra, rb, static_cast<int>(w), View{T1, w, 1}, View{cb, 1, w}, out, rb, 1, sh);
+}
+
+// als_local_update (detail/als_local_solve.hpp): X (lr, n, rc) = L Y_k R.
+__device__ void local_update(const double* L, int lr, const double* Y, int yr, int n, int yrp,
+                             const double* R, int rc, double* X, Bump bump, CtaShared& sh)
+{
+  const int64_t w = static_cast<int64_t>(n) * yrp;
+  double* T1 = bump.take(static_cast<int64_t>(lr) * w);
+  cta_gemm(lr, static_cast<int>(w), yr, View{L, yr, 1}, View{Y, w, 1}, T1, w, 1, sh);
+  cta_gemm(lr * n, rc, yrp, View{T1, yrp, 1}, View{R, rc, 1}, X, rc, 1, sh);
+}
+
+// merge_y_block (detail/dmrg_local_solve.hpp): Theta (rxl*n0, n1*rxr) =
+// (L Y_k) (Y_k1 R).
+__device__ double* merge_pair(const double* L, int rxl, const double* Y0, int yr0, int n0,
+                              int yr1, const double* Y1, int n1, int yr2, const double* R,
+                              int rxr, Bump& bump, CtaShared& sh)
+{
+  const int64_t w0 = static_cast<int64_t>(n0) * yr1;
+  const int64_t cols = static_cast<int64_t>(n1) * rxr;
+  double* T1 = bump.take(static_cast<int64_t>(rxl) * w0);
+  double* T2 = bump.take(static_cast<int64_t>(yr1) * cols);
+  double* Th = bump.take(static_cast<int64_t>(rxl) * n0 * cols);
+  cta_gemm(rxl, static_cast<int>(w0), yr0, View{L, yr0, 1}, View{Y0, w0, 1}, T1, w0, 1, sh);
+  cta_gemm(yr1 * n1, rxr, yr2, View{Y1, yr2, 1}, View{R, rxr, 1}, T2, rxr, 1, sh);
+  cta_gemm(rxl * n0, static_cast<int>(cols), yr1, View{T1, yr1, 1}, View{T2, cols, 1}, Th, cols,
+           1, sh);
+  return Th;
+}
+
+__device__ __noinline__ void iter_round_tt(const RoundJob& job, int item, double* scratch, Smem sm,
+                                           CtaShared& sh)
+{
+  const bool dmrg = job.kind == kJobDmrg;
+  TTInfo& TY = job.tts[job.a_idx[item]];
+  TTInfo& TX = job.tts[job.b_idx[item]];
+  const int d = TY.d;
+  CoreSlot* SY = job.slots + TY.first;
+  CoreSlot* SX = job.slots + TX.first;
+  double* ar = job.arena;
+  const int64_t es = TX.env_stride;
+  double* env = ar + TX.env_off;
+  // After the environments: cmax, s_prev, s_now ((d-1) x cmax each),
+  // cnt_prev, cnt_now (d-1 each), caps (d+1).
+  double* base2 = env + 2 * static_cast<int64_t>(d + 1) * es;
+  const int cmax = static_cast<int>(base2[0]);
+  double* sp = base2 + 1;
+  double* sn = sp + static_cast<int64_t>(d - 1) * cmax;
+  double* cp = sn + static_cast<int64_t>(d - 1) * cmax;
+  double* cn = cp + (d - 1);
+  const double* caps = cn + (d - 1);
+  auto Lk = [&](int k) { return env + static_cast<int64_t>(k) * es; };
+  auto Rk = [&](int k) { return env + static_cast<int64_t>(d + 1 + k) * es; };
+  auto core = [&](CoreSlot* S, int k) { return ar + S[k].off; };
+  double* sdummy = nullptr;
+
+  double delta = 0.0;
+  if (dmrg)
+  {
+    // ||Y|| by the inner chain of Y with itself (algebra/tt_inner.hpp:33-47).
+    if (threadIdx.x == 0)
+      Lk(0)[0] = 1.0;
+    __syncthreads();
+    for (int k = 0; k < d; ++k)
+      env_left(Lk(k), core(SY, k), SY[k].r, SY[k].n, SY[k].rp, core(SY, k), SY[k].r, SY[k].rp,
+               Lk(k + 1), Bump{scratch}, sh);
+    const double yy = Lk(d)[0];
+    const double ynorm = sqrt(yy > 0.0 ? yy : 0.0);
+    delta = job.eps * ynorm / sqrt(static_cast<double>(d - 1 > 1 ? d - 1 : 1));
+    if (threadIdx.x == 0)
+    {
+      TX.norm = ynorm;
+      TX.delta = delta;
+    }
+  }
+  if (!job.x_right_canonical)
+    for (int k = d - 1; k >= 1; --k)
+    {
+      if (!fits(job, need_right_qr(SX[k].r, static_cast<int64_t>(SX[k].n) * SX[k].rp,
+                                   static_cast<int64_t>(SX[k - 1].r) * SX[k - 1].n), TX))
+        return;
+      right_qr_step(ar, SX[k], SX[k - 1], Bump{scratch}, sm, false, sh);
+    }
+  if (threadIdx.x == 0)
+  {
+    Rk(d)[0] = 1.0;
+    Lk(0)[0] = 1.0;
+  }
+  __syncthreads();
+  for (int k = d - 1; k >= 1; --k)
+    env_right(core(SY, k), SY[k].r, SY[k].n, SY[k].rp, core(SX, k), SX[k].r, SX[k].rp, Rk(k + 1),
+              Rk(k), Bump{scratch}, sh);
+
+  int iters = 0, converged = 0;
+  double change = 0.0;
+  for (int it = 0; it < job.max_iters; ++it)
+  {
+    if (!dmrg)
+    {
+      for (int k = 0; k < d; ++k)
+      {
+        local_update(Lk(k), SX[k].r, core(SY, k), SY[k].r, SY[k].n, SY[k].rp, Rk(k + 1),
+                     SX[k].rp, core(SX, k), Bump{scratch}, sh);
+        if (k < d - 1)
+        {
+          if (!fits(job, need_left_qr(static_cast<int64_t>(SX[k].r) * SX[k].n, SX[k].rp,
+                                      static_cast<int64_t>(SX[k + 1].n) * SX[k + 1].rp), TX))
+            return;
+          left_qr_step(ar, SX[k], SX[k + 1], Bump{scratch}, sm, false, sh);
+          env_left(Lk(k), core(SX, k), SX[k].r, SX[k].n, SX[k].rp, core(SY, k), SY[k].r,
+                   SY[k].rp, Lk(k + 1), Bump{scratch}, sh);
+        }
+      }
+      for (int k = d - 1; k >= 0; --k)
+      {
+        if (k < d - 1)
+          local_update(Lk(k), SX[k].r, core(SY, k), SY[k].r, SY[k].n, SY[k].rp, Rk(k + 1),
+                       SX[k].rp, core(SX, k), Bump{scratch}, sh);
+        if (k > 0)
+        {
+          if (!fits(job, need_right_qr(SX[k].r, static_cast<int64_t>(SX[k].n) * SX[k].rp,
+                                       static_cast<int64_t>(SX[k - 1].r) * SX[k - 1].n), TX))
+            return;
+          right_qr_step(ar, SX[k], SX[k - 1], Bump{scratch}, sm, false, sh);
+          env_right(core(SY, k), SY[k].r, SY[k].n, SY[k].rp, core(SX, k), SX[k].r, SX[k].rp,
+                    Rk(k + 1), Rk(k), Bump{scratch}, sh);
+        }
+      }
+      // Bond spectra of the cores (core_singular_values, tt_als.hpp:170-190).
+      for (int k = 0; k < d - 1; ++k)
+      {
+        const int h = SX[k].r * SX[k].n, c = SX[k].rp;
+        if (!fits(job, need_left_svd(h, c) + a32(static_cast<int64_t>(h) * c), TX))
+          return;
+        double *U, *F, *sv;
+        left_svd(View{core(SX, k), c, 1}, h, c, 0.0, 0, job.max_sweeps, false, Bump{scratch}, sm,
+                 &U, &F, TX, sh, nullptr, &sv);
+        const int cnt = h < c ? h : c;
+        for (int i = threadIdx.x; i < cnt; i += blockDim.x)
+          sn[static_cast<int64_t>(k) * cmax + i] = sv[i];
+        if (threadIdx.x == 0)
+          cn[k] = cnt;
+        __syncthreads();
+      }
+    }
+    else
+    {
+      for (int k = 0; k < d - 1; ++k)
+      {
+        const int rxl = SX[k].r, rxr = SX[k + 1].rp, n0 = SY[k].n, n1 = SY[k + 1].n;
+        const int rows = rxl * n0, cols = n1 * rxr;
+        const int cap = static_cast<int>(caps[k + 1]);
+        const int mr = job.max_rank > 0 && job.max_rank < cap ? job.max_rank : cap;
+        if (!fits(job, a32(static_cast<int64_t>(rxl) * n0 * SY[k].rp) +
+                         a32(static_cast<int64_t>(SY[k].rp) * cols) +
+                         a32(static_cast<int64_t>(rows) * cols) + need_left_svd(rows, cols),
+                  TX))
+          return;
+        Bump bump{scratch};
+        double* Th = merge_pair(Lk(k), rxl, core(SY, k), SY[k].r, n0, SY[k].rp, core(SY, k + 1),
+                                n1, SY[k + 1].rp, Rk(k + 2), rxr, bump, sh);
+        double *U, *F, *sv;
+        const int r = left_svd(View{Th, cols, 1}, rows, cols, delta, mr, job.max_sweeps, false,
+                               bump, sm, &U, &F, TX, sh, nullptr, &sv);
+        // X_k <- U, X_k1 <- diag(s) V^T (split_two_site_lr).
+        cta_copy_to_rowmajor(core(SX, k), r, View{U, 1, rows}, rows, r);
+        cta_copy(core(SX, k + 1), F, static_cast<int64_t>(r) * cols);
+        set_ranks(SX[k], rxl, r);
+        set_ranks(SX[k + 1], r, rxr);
+        for (int i = threadIdx.x; i < r; i += blockDim.x)
+          sn[static_cast<int64_t>(k) * cmax + i] = sv[i];
+        if (threadIdx.x == 0)
+          cn[k] = r;
+        __syncthreads();
+        env_left(Lk(k), core(SX, k), SX[k].r, SX[k].n, SX[k].rp, core(SY, k), SY[k].r, SY[k].rp,
+                 Lk(k + 1), Bump{scratch}, sh);
+      }
+      for (int k = d - 2; k >= 0; --k)
+      {
+        const int rxl = SX[k].r, rxr = SX[k + 1].rp, n0 = SY[k].n, n1 = SY[k + 1].n;
+        const int rows = rxl * n0, cols = n1 * rxr;
+        const int cap = static_cast<int>(caps[k + 1]);
+        const int mr = job.max_rank > 0 && job.max_rank < cap ? job.max_rank : cap;
+        if (!fits(job, a32(static_cast<int64_t>(rxl) * n0 * SY[k].rp) +
+                         a32(static_cast<int64_t>(SY[k].rp) * cols) +
+                         a32(static_cast<int64_t>(rows) * cols) + need_left_svd(cols, rows),
+                  TX))
+          return;
+        Bump bump{scratch};
+        double* Th = merge_pair(Lk(k), rxl, core(SY, k), SY[k].r, n0, SY[k].rp, core(SY, k + 1),
+                                n1, SY[k + 1].rp, Rk(k + 2), rxr, bump, sh);
+        // split_two_site_rl through Theta^T = V S U^T: U' = V, F' = S U^T.
+        double *U, *F;
+        const int r = left_svd(View{Th, 1, cols}, cols, rows, delta, mr, job.max_sweeps, false,
+                               bump, sm, &U, &F, TX, sh, nullptr, &sdummy);
+        cta_copy(core(SX, k + 1), U, static_cast<int64_t>(r) * cols);         // V^T
+        cta_copy_to_rowmajor(core(SX, k), r, View{F, 1, rows}, rows, r);    // U diag(s)
+        set_ranks(SX[k], rxl, r);
+        set_ranks(SX[k + 1], r, rxr);
+        __syncthreads();
+        env_right(core(SY, k + 1), SY[k + 1].r, SY[k + 1].n, SY[k + 1].rp, core(SX, k + 1),
+                  SX[k + 1].r, SX[k + 1].rp, Rk(k + 2), Rk(k + 1), Bump{scratch}, sh);
+      }
+    }
+    ++iters;
+    // Largest relative change of the bond spectra (sv_change; a bond whose
+    // count changed counts as 1, as tt_als.hpp:182-186 / tt_dmrg.hpp do).
+    if (threadIdx.x == 0)
+    {
+      double worst = 0.0;
+      for (int k = 0; k < d - 1; ++k)
+      {
+        const int a = static_cast<int>(cn[k]), b = static_cast<int>(cp[k]);
+        if (it == 0)
+          continue;
+        if (a != b)
+        {
+          worst = 1.0;
+          continue;
+        }
+        double dn = 0.0, nn = 0.0;
+        for (int i = 0; i < a; ++i)
+        {
+          const double x = sn[static_cast<int64_t>(k) * cmax + i];
+          const double y = sp[static_cast<int64_t>(k) * cmax + i];
+          dn += (x - y) * (x - y);
+          nn += x * x;
+        }
+        const double rel = sqrt(dn) / (sqrt(nn) + 1.0e-300);
+        worst = rel > worst ? rel : worst;
+      }
+      sh.dval[0] = it == 0 ? 1.0 : worst;
+    }
+    __syncthreads();
+    change = sh.dval[0];
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(d - 1) * (cmax + 1); t += blockDim.x)
+    {
+      if (t < static_cast<int64_t>(d - 1) * cmax)
+        sp[t] = sn[t];
+      else
+        cp[t - static_cast<int64_t>(d - 1) * cmax] = cn[t - static_cast<int64_t>(d - 1) * cmax];
+    }
+    __syncthreads();
+    if (change <= job.tol)
+    {
+      converged = 1;
+      break;
+    }
+  }
+  if (threadIdx.x == 0)
+  {
+    TX.iters_run = iters;
+    TX.iter_conv = converged;
+    TX.final_change = change;
+  }
+  __syncthreads();
+}
+
 template <int MinBlocks>
 __global__ void __launch_bounds__(kThreads, MinBlocks) round_kernel(RoundJob job)
 {
@@ -1066,6 +1382,8 @@ __global__ void __launch_bounds__(kThreads, MinBlocks) round_kernel(RoundJob job
       stream_tt(job, job.order[item], scratch, sm, sh);
     else if (job.kind == kJobRoundSketch)
       round_sketch_tt(job, job.order[item], scratch, sm, sh);
+    else if (job.kind == kJobAls || job.kind == kJobDmrg)
+      iter_round_tt(job, job.order[item], scratch, sm, sh);
     else
       round_tt(job, job.order[item], scratch, sm, sh, job.eps);
   }

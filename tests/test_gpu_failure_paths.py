@@ -53,14 +53,18 @@ def test_nan_core_reported(ttg, prec, schedule):
     _good(ttg)
 
 
-def test_sweep_limit_reported(ttg):
+@pytest.mark.parametrize("schedule", ["per_tt", "whole_gpu"])
+def test_sweep_limit_reported(ttg, schedule):
+    # max_rank below the bond ranks forces truncation, so every bond runs
+    # its Jacobi SVD; one sweep cannot converge on rank-64 bonds.
     t = O.random([4] * 8, 64, 11, fan_in_scale=True)
     info = ttg.RoundResult()
-    y = ttg.round(t, ttg.RoundOptions(eps=1e-8, max_sweeps=1), info)
+    sch = ttg.schedule[schedule]
+    y = ttg.round(t, ttg.RoundOptions(eps=1e-8, max_sweeps=1, max_rank=48, schedule=sch), info)
     assert not info.converged and info.status == 6
     assert all(np.isfinite(c).all() for c in y)
     info2 = ttg.RoundResult()
-    ttg.round(t, ttg.RoundOptions(eps=1e-8), info2)
+    ttg.round(t, ttg.RoundOptions(eps=1e-8, max_rank=48, schedule=sch), info2)
     assert info2.converged and info2.status == 0
 
 
