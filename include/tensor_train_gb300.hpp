@@ -16,6 +16,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <utility>
 #include <vector>
 
@@ -406,6 +407,29 @@ inline void fill(const ttg_round_result& r, round_result* info)
   info->converged = r.converged != 0;
 }
 
+inline bool iterative(const round_options& o)
+{
+  return o.method == round_method::als || o.method == round_method::dmrg;
+}
+
+// The iterative fields of round_options (round.hpp:84-104) with the warm
+// start that matches the call's type (tt or tt_matrix), kept alive here.
+struct iter_args
+{
+  std::unique_ptr<flat> warm;
+  ttg_iter_options c{};
+  template <class W>
+  iter_args(const round_options& o, const W* w)
+  {
+    if (w)
+      warm.reset(new flat(*w));
+    c.max_iters = o.max_iters;
+    c.tol = o.tol;
+    c.seed = o.seed;
+    c.warm = warm ? &warm->t : nullptr;
+  }
+};
+
 }  // namespace detail
 
 // ---- factories (factory/tt_factory.hpp, factory/tt_matrix_factory.hpp) ----
@@ -478,15 +502,21 @@ inline tt scale(const tt& a, double alpha)
 }
 
 // ---- the hot path -------------------------------------------------------
-// round (round/round.hpp:230-312): svd method on the GPU; als/dmrg are not
-// served by this library and abort like an unknown method.
+// round (round/round.hpp:230-312): every method on the GPU (svd; als and
+// dmrg through ttg_round_iter with the options' iterative fields).
 inline tt round(const tt& a, const round_options& opts, round_result* info = nullptr)
 {
   detail::flat in(a);
   detail::owned out;
   ttg_round_options o = detail::to_c(opts);
   ttg_round_result r{};
-  detail::check(ttg_round(&in.t, &o, &out.t, &r), "round(tt)");
+  if (detail::iterative(opts))
+  {
+    detail::iter_args it(opts, opts.warm_start_tt);
+    detail::check(ttg_round_iter(&in.t, &o, &it.c, &out.t, &r), "round(tt)");
+  }
+  else
+    detail::check(ttg_round(&in.t, &o, &out.t, &r), "round(tt)");
   detail::fill(r, info);
   return detail::to_tt(out.t);
 }
@@ -503,7 +533,13 @@ inline tt_matrix round(const tt_matrix& a, const round_options& opts, round_resu
   detail::owned out;
   ttg_round_options o = detail::to_c(opts);
   ttg_round_result r{};
-  detail::check(ttg_round(&in.t, &o, &out.t, &r), "round(tt_matrix)");
+  if (detail::iterative(opts))
+  {
+    detail::iter_args it(opts, opts.warm_start_tt_matrix);
+    detail::check(ttg_round_iter(&in.t, &o, &it.c, &out.t, &r), "round(tt_matrix)");
+  }
+  else
+    detail::check(ttg_round(&in.t, &o, &out.t, &r), "round(tt_matrix)");
   detail::fill(r, info);
   return detail::to_tt_matrix(out.t);
 }
@@ -521,7 +557,13 @@ inline tt matvec_round(const tt_matrix& a, const tt& x, const round_options& opt
   detail::owned out;
   ttg_round_options o = detail::to_c(opts);
   ttg_round_result r{};
-  detail::check(ttg_matvec_round(&fa.t, &fx.t, &o, &out.t, &r), "matvec_round");
+  if (detail::iterative(opts))
+  {
+    detail::iter_args it(opts, opts.warm_start_tt);
+    detail::check(ttg_apply_round_iter(&fa.t, &fx.t, &o, &it.c, &out.t, &r), "matvec_round");
+  }
+  else
+    detail::check(ttg_matvec_round(&fa.t, &fx.t, &o, &out.t, &r), "matvec_round");
   detail::fill(r, info);
   return detail::to_tt(out.t);
 }
@@ -534,7 +576,13 @@ inline tt_matrix matmat_round(const tt_matrix& a, const tt_matrix& b, const roun
   detail::owned out;
   ttg_round_options o = detail::to_c(opts);
   ttg_round_result r{};
-  detail::check(ttg_matmat_round(&fa.t, &fb.t, &o, &out.t, &r), "matmat_round");
+  if (detail::iterative(opts))
+  {
+    detail::iter_args it(opts, opts.warm_start_tt_matrix);
+    detail::check(ttg_apply_round_iter(&fa.t, &fb.t, &o, &it.c, &out.t, &r), "matmat_round");
+  }
+  else
+    detail::check(ttg_matmat_round(&fa.t, &fb.t, &o, &out.t, &r), "matmat_round");
   detail::fill(r, info);
   return detail::to_tt_matrix(out.t);
 }

@@ -45,7 +45,7 @@ typedef enum ttg_status {
   TTG_ERR_NO_SPACE = 11      /* a size exceeds a fixed capacity */
 } ttg_status;
 
-/* round_method (round/round.hpp:33-44).  als/dmrg are not served here. */
+/* round_method (round/round.hpp:33-44). */
 typedef enum ttg_method {
   TTG_METHOD_SVD = 0,
   TTG_METHOD_SVD_STREAMING = 1,
@@ -148,9 +148,43 @@ void ttg_free(ttg_tensor* t);
  *           overloads (round.hpp:329-425, via pack/unpack
  *           round/tt_matrix_round.hpp:27-72) when in->cols != NULL.
  * Rejects svd_streaming / svd_naive like round_assert_method_for_value
- * (round.hpp:124-134); ALS/DMRG are out of scope (TTG_ERR_METHOD). */
+ * (round.hpp:124-134).  Method ALS / DMRG runs the engine of ttg_round_iter
+ * with its default iteration options. */
 int32_t ttg_round(const ttg_tensor* in, const ttg_round_options* opts, ttg_tensor* out,
                   ttg_round_result* result);
+
+/* ALS and two-site DMRG rounding.
+ * Replaces: round(tt, opts) with method als / dmrg (round/round.hpp:230-266
+ *           -> round/tt_als.hpp:212-300, round/tt_dmrg.hpp:217-300) and the
+ *           tt_matrix overloads (round/tt_matrix_als_round.hpp,
+ *           tt_matrix_dmrg_round.hpp), with the iterative fields of
+ *           round_options (round.hpp:84-104) in ttg_iter_options.
+ * ttg_round / ttg_matvec_round / ttg_matmat_round with method ALS or DMRG
+ * use the defaults below.  Start TT as the reference picks it: a compatible
+ * warm start; for ALS without max_rank the SVD round at eps (its largest
+ * rank becomes max_rank); else round_right_canonical (ALS at eps 0, DMRG at
+ * eps) -- or, in ttg_apply_round_iter and the matvec/matmat entries,
+ * random(shape, max_rank, seed) when a max_rank is known.  FP64 only.
+ * round_result: iters_run, converged, final_resid = the last change of the
+ * bond spectra.  DMRG keeps at most min(Y's bond rank, max_rank) per bond
+ * (the merged pair has no larger rank; further singular values are
+ * rounding noise). */
+typedef struct ttg_iter_options {
+  int32_t max_iters;      /* sweep pairs, 0 = 20 */
+  int32_t reserved;
+  double tol;             /* stop when the spectra change by <= tol; 0 = 1e-12 */
+  uint64_t seed;          /* random start of the apply variants */
+  const ttg_tensor* warm; /* optional warm start (same modes), borrowed */
+} ttg_iter_options;
+int32_t ttg_round_iter(const ttg_tensor* in, const ttg_round_options* opts,
+                       const ttg_iter_options* iter, ttg_tensor* out, ttg_round_result* result);
+/* Replaces: matvec_round / matmat_round with method als / dmrg
+ * (round/tt_matvec_als_round.hpp, tt_matvec_dmrg_round.hpp,
+ * tt_matmat_als_round.hpp, tt_matmat_dmrg_round.hpp): y = round(A x) by the
+ * iterative method from a random start (x a TT-matrix: matmat). */
+int32_t ttg_apply_round_iter(const ttg_tensor* A, const ttg_tensor* x,
+                             const ttg_round_options* opts, const ttg_iter_options* iter,
+                             ttg_tensor* out, ttg_round_result* result);
 
 /* Many independent TTs (uneven d, n, ranks) rounded in one persistent
  * launch.  No reference counterpart takes a batch; each element follows

@@ -81,6 +81,12 @@ class RoundOptions:
     sketch_ranks: object = None   # per-bond sketch ranks, TT by TT (method = sketch)
     sketch_seed: int = 0
     bond_stats: object = None     # numpy float64 array (4 per bond) filled by the exact rounder
+    # ALS / DMRG (method als / dmrg): round_options::max_iters, tol, seed,
+    # warm_start_tt / warm_start_tt_matrix (round/round.hpp:84-104)
+    max_iters: int = 20
+    tol: float = 1e-12
+    seed: int = 0
+    warm: object = None           # list of cores (same modes), or None
 
 
 @dataclasses.dataclass
@@ -118,6 +124,11 @@ class _Tensor(C.Structure):
                 ("rows", C.POINTER(C.c_int32)), ("cols", C.POINTER(C.c_int32)),
                 ("offsets", C.POINTER(C.c_int64)), ("data", C.POINTER(C.c_double)),
                 ("owned", C.c_int32)]
+
+
+class _Iter(C.Structure):
+    _fields_ = [("max_iters", C.c_int32), ("reserved", C.c_int32), ("tol", C.c_double),
+                ("seed", C.c_uint64), ("warm", C.POINTER(_Tensor))]
 
 
 _lib = None
@@ -179,6 +190,8 @@ def lib():
         "ttg_plan_schedule": (C.c_int32, [C.c_void_p]),
         "ttg_plan_graph": (C.c_int32, [C.c_void_p, C.c_int32]),
         "ttg_plan_autotune": (C.c_int32, [C.c_void_p, C.c_void_p, C.POINTER(C.c_int32)]),
+        "ttg_round_iter": (C.c_int32, [T, O, C.POINTER(_Iter), T, R]),
+        "ttg_apply_round_iter": (C.c_int32, [T, T, O, C.POINTER(_Iter), T, R]),
         "ttg_shard_plan": (C.c_int32, [C.c_int32, T, C.c_int32, C.POINTER(C.c_int32),
                                        C.POINTER(C.c_double)]),
         "ttg_round_batch_devices": (C.c_int32, [C.c_int32, T, O, T, R, C.c_int32,
@@ -290,7 +303,12 @@ def round(a, opts: RoundOptions | None = None, info: RoundResult | None = None):
     src = _In(a)
     out, res = _Tensor(), _Result()
     o = _opts(opts)
-    st = lib().ttg_round(C.byref(src.t), C.byref(o), C.byref(out), C.byref(res))
+    if _iterative(opts):
+        it, keep = _iter_opts(opts)
+        st = lib().ttg_round_iter(C.byref(src.t), C.byref(o), C.byref(it), C.byref(out),
+                                  C.byref(res))
+    else:
+        st = lib().ttg_round(C.byref(src.t), C.byref(o), C.byref(out), C.byref(res))
     if st != 0 and out.owned:
         lib().ttg_free(C.byref(out))
     _check(st, "round")
@@ -351,11 +369,31 @@ def soft_threshold(a, tau=0.0):
     return _take(out)
 
 
+def _iterative(opts) -> bool:
+    return opts is not None and int(opts.method) in (int(round_method.als),
+                                                      int(round_method.dmrg))
+
+
+def _iter_opts(opts):
+    """(ttg_iter_options, keep-alive) of an ALS / DMRG call."""
+    it = _Iter(int(opts.max_iters), 0, float(opts.tol), int(opts.seed), None)
+    keep = None
+    if opts.warm is not None:
+        keep = _In(opts.warm)
+        it.warm = C.pointer(keep.t)
+    return it, keep
+
+
 def _apply_round(fn, what, A, X, opts, info):
     sa, sx = _In(A), _In(X)
     out, res = _Tensor(), _Result()
     o = _opts(opts)
-    st = fn(C.byref(sa.t), C.byref(sx.t), C.byref(o), C.byref(out), C.byref(res))
+    if _iterative(opts):
+        it, keep = _iter_opts(opts)
+        st = lib().ttg_apply_round_iter(C.byref(sa.t), C.byref(sx.t), C.byref(o), C.byref(it),
+                                        C.byref(out), C.byref(res))
+    else:
+        st = fn(C.byref(sa.t), C.byref(sx.t), C.byref(o), C.byref(out), C.byref(res))
     if st != 0 and out.owned:
         lib().ttg_free(C.byref(out))
     _check(st, what)

@@ -61,7 +61,7 @@ class RoundOptions:
     (round/round.hpp:55-105): eps (0.0), max_rank (0 = no cap), method
     ("svd"; "svd_streaming" for matvec_round, "svd_naive" for matmat_round),
     gauge ("none" or "right_canonical"), max_iters, tol, seed and warm_start
-    (ALS/DMRG only; stored and type-checked).  Keyword arguments or one
+    (ALS/DMRG only).  Keyword arguments or one
     dict.  Also accepted: precision ("fp64" or "mixed"), schedule
     ("auto", "per_tt", "whole_gpu", "teams") and max_sweeps."""
 
@@ -84,6 +84,9 @@ class RoundOptions:
     def _as_c(self, **overrides) -> _COptions:
         o = _COptions()
         fields = dict((k, getattr(self, k)) for k in _C_FIELDS if hasattr(self, k))
+        warm = getattr(self, "warm_start", None)
+        if warm is not None:
+            fields["warm"] = list(warm._cores)
         fields.update((k, v) for k, v in overrides.items() if k in _C_FIELDS)
         for k, v in fields.items():
             if k == "method":
@@ -102,7 +105,8 @@ class RoundOptions:
 
 # Options forwarded to the library: the reference's SVD-path fields, plus
 # this library's precision ("fp64" / "mixed"), schedule and Jacobi sweep cap.
-_C_FIELDS = ("eps", "max_rank", "method", "gauge", "precision", "schedule", "max_sweeps")
+_C_FIELDS = ("eps", "max_rank", "method", "gauge", "precision", "schedule", "max_sweeps",
+             "max_iters", "tol", "seed", "warm")
 
 
 def _options(opts, kwargs) -> _COptions:
@@ -111,12 +115,8 @@ def _options(opts, kwargs) -> _COptions:
     if isinstance(opts, RoundOptions):
         return opts._as_c(**kwargs)
     if isinstance(opts, dict):
-        d = dict(opts)
-        d.pop("warm_start", None)
-        return RoundOptions(**d)._as_c()
-    kwargs = dict(kwargs)
-    kwargs.pop("warm_start", None)
-    return RoundOptions(**kwargs)._as_c()
+        return RoundOptions(**dict(opts))._as_c()
+    return RoundOptions(**dict(kwargs))._as_c()
 
 
 class RoundResult:

@@ -275,6 +275,10 @@ struct ttg_plan
     int a_slot, x_slot, y_slot, r, m, p, rp, s, nout, sp;
   };
   std::vector<Apply> applies;
+  // iterative rounding (ALS / DMRG)
+  int iter_max = 20;
+  double iter_tol = 1.0e-12;
+  bool iter_rc = false;
   // whole-GPU schedule (wide_round_kernel)
   bool wide = false;
   int wide_grid = 0;
@@ -709,6 +713,9 @@ RoundJob make_job(ttg_plan& P)
   j.pristine_arena = reinterpret_cast<const double*>(d + P.off_pristine + P.off_arena);
   j.pristine_slots = reinterpret_cast<const CoreSlot*>(d + P.off_pristine + P.off_slots);
   j.bond_stats = P.opts.bond_stats ? reinterpret_cast<BondStat*>(d + P.off_stats) : nullptr;
+  j.max_iters = P.iter_max;
+  j.tol = P.iter_tol;
+  j.x_right_canonical = P.iter_rc ? 1 : 0;
   return j;
 }
 
@@ -726,8 +733,6 @@ int32_t check_opts(const ttg_round_options* o, const char* op)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown precision");
   if (o->schedule < TTG_SCHED_AUTO || o->schedule > TTG_SCHED_TEAMS)
     return fail(TTG_ERR_ARG, std::string(op) + ": unknown schedule");
-  if (o->method == TTG_METHOD_ALS || o->method == TTG_METHOD_DMRG)
-    return fail(TTG_ERR_METHOD, std::string(op) + ": als/dmrg rounding is not served here");
   if (o->method < 0 || o->method > TTG_METHOD_SKETCH)
     return fail(TTG_ERR_METHOD, std::string(op) + ": unknown method " + std::to_string(o->method));
   return TTG_OK;
@@ -1412,6 +1417,294 @@ int32_t ttg_plan_download(ttg_plan* P, void* stream, ttg_tensor* outs, double* v
                               : TTG_OK;
 }
 
+// --------------------------------------------------------------------------
+// ALS / two-site DMRG rounding (round/tt_als.hpp:212-300,
+// round/tt_dmrg.hpp:217-300, and their matvec/matmat variants): the start TT
+// is chosen on the host exactly as the reference chooses it (warm start,
+// SVD round, round_right_canonical or a random TT), then one CTA runs the
+// sweeps on the device (kJobAls / kJobDmrg, iter_round_tt).
+// --------------------------------------------------------------------------
+struct TensorView
+{
+  std::vector<int32_t> ranks, rows, cols;
+  std::vector<int64_t> offsets;
+  ttg_tensor t{};
+  // A view of s with its column modes folded into the row modes (the packed
+  // 3-axis cores of a TT-matrix) when `pack`.
+  TensorView(const Shape& s, bool pack)
+  {
+    ranks.assign(s.r.begin(), s.r.end());
+    if (ranks.empty())
+      ranks.push_back(1);
+    for (int k = 0; k < s.d; ++k)
+    {
+      rows.push_back(pack ? s.mode(k) : s.m[k]);
+      cols.push_back(s.n[k]);
+      offsets.push_back(s.src_off[k]);
+    }
+    offsets.push_back(s.d > 0 ? s.src_off[s.d - 1] + s.size[s.d - 1] : 0);
+    t.d = s.d;
+    t.ranks = ranks.data();
+    t.rows = rows.empty() ? nullptr : rows.data();
+    t.cols = (s.matrix && !pack) ? cols.data() : nullptr;
+    t.offsets = offsets.data();
+    t.data = const_cast<double*>(s.data);
+  }
+};
+
+struct OwnedTensor
+{
+  ttg_tensor t{};
+  ~OwnedTensor() { ttg_free(&t); }
+};
+
+int max_rank_of(const ttg_tensor& t)
+{
+  int m = 0;
+  for (int k = 0; k <= t.d; ++k)
+    m = std::max(m, t.ranks[k]);
+  return m;
+}
+
+// Bond capacities of the start TT in DMRG: a merged pair L Y_k Y_k1 R has
+// rank <= Y's middle rank, and the split keeps at most max_rank and what the
+// unfolding allows; the start TT's own ranks always fit.
+std::vector<int> dmrg_caps(const Shape& Y, const std::vector<int>& rx, int max_rank)
+{
+  const int d = Y.d;
+  std::vector<int> cap(static_cast<size_t>(d + 1), 1);
+  std::vector<double> left(static_cast<size_t>(d + 1), 1.0), right(static_cast<size_t>(d + 1), 1.0);
+  for (int k = 0; k < d; ++k)
+    left[k + 1] = std::min(left[k] * Y.mode(k), 1e18);
+  for (int k = d - 1; k >= 0; --k)
+    right[k] = std::min(right[k + 1] * Y.mode(k), 1e18);
+  for (int k = 1; k < d; ++k)
+  {
+    double c = std::min({static_cast<double>(Y.r[k]), left[k], right[k]});
+    if (max_rank > 0)
+      c = std::min(c, static_cast<double>(max_rank));
+    cap[k] = std::max(rx[k], static_cast<int>(c));
+  }
+  return cap;
+}
+
+int32_t run_iter_engine(const Shape& Y, const ttg_tensor& X0, bool dmrg, bool rc, int max_rank,
+                        double eps, int max_iters, double tol, ttg_tensor* out,
+                        ttg_round_result* result, const char* op)
+{
+  Shape XS;
+  if (int32_t st = describe(&X0, op, XS))
+    return st;
+  if (XS.d != Y.d)
+    return fail(TTG_ERR_SHAPE, std::string(op) + ": start TT has a different order");
+  const int d = Y.d;
+  std::vector<int> rx(XS.r.begin(), XS.r.end());
+  const std::vector<int> cap = dmrg ? dmrg_caps(Y, rx, max_rank) : rx;
+  std::vector<int> ry(Y.r.begin(), Y.r.end()), nm(static_cast<size_t>(d));
+  for (int k = 0; k < d; ++k)
+    nm[k] = Y.mode(k);
+  int cmax = 1, rymax = 1;
+  for (int k = 0; k <= d; ++k)
+  {
+    cmax = std::max(cmax, cap[k]);
+    rymax = std::max(rymax, ry[k]);
+  }
+  std::lock_guard<std::mutex> lk(dev_state().mu);
+  ttg_plan P;
+  PoolLease lease(P);
+  P.opts = ttg_round_options{};
+  P.opts.eps = eps;
+  P.opts.max_rank = max_rank;
+  P.opts.method = dmrg ? TTG_METHOD_DMRG : TTG_METHOD_ALS;
+  P.kind = kPlanRound;
+  P.job_kind = dmrg ? kJobDmrg : kJobAls;
+  P.iter_max = max_iters;
+  P.iter_tol = tol;
+  P.iter_rc = rc;
+  // Y as a plain TT of its packed modes; X in slots of capacity cap_k n_k cap_k+1.
+  Shape Yp = Y;
+  if (Yp.matrix)
+  {
+    for (int k = 0; k < d; ++k)
+    {
+      Yp.m[k] = Y.mode(k);
+      Yp.n[k] = 1;
+    }
+    Yp.matrix = false;
+  }
+  Shape Xp = XS;
+  Xp.matrix = false;
+  for (int k = 0; k < d; ++k)
+  {
+    Xp.m[k] = XS.mode(k);
+    Xp.n[k] = 1;
+  }
+  P.shapes = {Yp, Xp};
+  add_tensor(P, Yp, true, nullptr);
+  std::vector<int64_t> xcap(static_cast<size_t>(d));
+  for (int k = 0; k < d; ++k)
+    xcap[k] = static_cast<int64_t>(cap[k]) * nm[k] * cap[k + 1];
+  add_tensor(P, Xp, true, &xcap);
+  // The pair's environments, spectra and capacities after the cores.
+  const int64_t es = a32(static_cast<int64_t>(std::max(cmax, rymax)) * rymax);
+  const int64_t tail = 1 + 2 * static_cast<int64_t>(d - 1) * cmax + 2 * (d - 1) + (d + 1);
+  const int64_t env_off = P.arena_doubles;
+  P.arena_doubles += a32(2 * static_cast<int64_t>(d + 1) * es + tail);
+  P.tts[1].env_off = env_off;
+  P.tts[1].env_stride = es;
+  P.order = {0};
+  P.a_idx = {0};
+  P.b_idx = {1};
+  P.out_idx = {1};
+  P.out_tts = {1};
+  P.scratch_stride = need_iter(d, ry.data(), nm.data(), cap.data(), dmrg);
+  P.grid = 1;
+  if (int32_t st = layout_and_alloc(P))
+    return st;
+  double* tailp = reinterpret_cast<double*>(static_cast<char*>(P.host.p) + P.off_arena) +
+                  env_off + 2 * static_cast<int64_t>(d + 1) * es;
+  std::memset(tailp, 0, sizeof(double) * static_cast<size_t>(tail));
+  tailp[0] = cmax;
+  for (int k = 0; k <= d; ++k)
+    tailp[tail - (d + 1) + k] = cap[k];
+  float ms = 0.0f;
+  if (int32_t st = execute(P, &ms))
+    return st;
+  if (int32_t st = emit_tensor(P, 1, Y.matrix, Y.m, Y.n, out))
+    return st;
+  const char* h = static_cast<const char*>(P.host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  if (result)
+  {
+    fill_result(T[1], ms, result);
+    result->iters_run = T[1].iters_run;
+    result->converged = T[1].iter_conv;
+    result->final_resid = T[1].final_change;
+  }
+  if (int32_t bad = first_bad_status(P))
+  {
+    ttg_free(out);
+    return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
+  }
+  return TTG_OK;
+}
+
+bool warm_compatible(const ttg_tensor* w, const Shape& Y)
+{
+  if (!w || w->d != Y.d || (w->cols != nullptr) != Y.matrix)
+    return false;
+  for (int k = 0; k < Y.d; ++k)
+  {
+    if (!w->rows || w->rows[k] != Y.m[k])
+      return false;
+    if (Y.matrix && w->cols[k] != Y.n[k])
+      return false;
+  }
+  return true;
+}
+
+// The reference's start-TT rules, then the device engine.  cold_random: the
+// matvec/matmat variants (round/tt_matvec_als_round.hpp:88-95 and the
+// DMRG/matmat ones) start from random(shape, max_rank, seed).
+int32_t round_iter_impl(const ttg_tensor* in, const ttg_round_options* opts,
+                        const ttg_iter_options* it, bool cold_random, ttg_tensor* out,
+                        ttg_round_result* result, const char* op)
+{
+  const bool dmrg = opts->method == TTG_METHOD_DMRG;
+  const char* nm = dmrg ? "dmrg_round" : "als_round";
+  if (dmrg && (std::isnan(opts->eps) || opts->eps <= 0.0))
+    return fail(TTG_ERR_ARG, std::string(nm) + ": eps must be > 0 for DMRG compression");
+  if (!dmrg && std::isnan(opts->eps))
+    return fail(TTG_ERR_ARG, std::string(nm) + ": eps is NaN; must be a valid number");
+  if (opts->gauge != TTG_GAUGE_NONE)
+    return fail(TTG_ERR_ARG, std::string(op) + ": gauge is an svd-method option");
+  if (opts->precision != TTG_PREC_FP64)
+    return fail(TTG_ERR_METHOD, std::string(op) + ": ALS / DMRG run in FP64 only");
+  const int max_iters = it && it->max_iters > 0 ? it->max_iters : 20;
+  const double tol = it && it->tol > 0.0 ? it->tol : 1.0e-12;
+  const uint64_t seed = it ? it->seed : 0;
+  const ttg_tensor* warm = it ? it->warm : nullptr;
+  Shape Y;
+  if (int32_t st = describe(in, op, Y))
+    return st;
+  if (int32_t st = need_device())
+    return st;
+  ttg_round_options svd{};
+  svd.eps = opts->eps;
+  svd.max_rank = opts->max_rank;
+  svd.method = TTG_METHOD_SVD;
+  svd.max_sweeps = opts->max_sweeps;
+  if (Y.d <= 1)
+  {
+    // d <= 1: the SVD round (tt_als.hpp:222-228, tt_dmrg.hpp:226-232).
+    if (int32_t st = ttg_round(in, &svd, out, nullptr))
+      return st;
+    if (result)
+    {
+      std::memset(result, 0, sizeof(*result));
+      result->converged = 1;
+    }
+    return TTG_OK;
+  }
+  const bool wc = warm_compatible(warm, Y);
+  int max_rank = opts->max_rank;
+  OwnedTensor ref, start;
+  const ttg_tensor* X0 = nullptr;
+  bool rc = false;
+  TensorView packed(Y, true);
+  if (!dmrg && max_rank <= 0)
+  {
+    if (opts->eps <= 0.0)
+      return fail(TTG_ERR_ARG, std::string(nm) + ": max_rank <= 0 and eps <= 0; ALS requires "
+                               "either max_rank > 0 or eps > 0 to determine compression target");
+    if (int32_t st = ttg_round(&packed.t, &svd, &ref.t, nullptr))
+      return st;
+    max_rank = max_rank_of(ref.t);
+    if (!wc)
+      X0 = &ref.t;
+  }
+  if (wc)
+  {
+    // (ALS always has a max_rank here: given, or taken from the SVD round.)
+    if (max_rank > 0)
+      for (int k = 0; k <= warm->d; ++k)
+        if (warm->ranks[k] > max_rank)
+          return fail(TTG_ERR_ARG, std::string(nm) + ": warm_start max rank " +
+                                       std::to_string(warm->ranks[k]) + " exceeds max_rank " +
+                                       std::to_string(max_rank));
+    X0 = warm;
+  }
+  if (!X0)
+  {
+    if (cold_random && (!dmrg || max_rank > 0))
+    {
+      if (int32_t st = ttg_host_random(Y.d, packed.rows.data(), nullptr, max_rank, seed, 0,
+                                       &start.t))
+        return fail(st, ttg_host_last_error());
+    }
+    else
+    {
+      ttg_round_options rco{};
+      rco.eps = dmrg ? opts->eps : 0.0;
+      rco.max_rank = max_rank;
+      rco.method = TTG_METHOD_SVD;
+      rco.gauge = TTG_GAUGE_RIGHT_CANONICAL;
+      rco.max_sweeps = opts->max_sweeps;
+      if (int32_t st = ttg_round(&packed.t, &rco, &start.t, nullptr))
+        return st;
+      rc = true;
+    }
+    X0 = &start.t;
+  }
+  // A warm start of a TT-matrix arrives with its 4-axis modes: view it packed.
+  Shape W;
+  if (int32_t st = describe(X0, op, W))
+    return st;
+  TensorView xview(W, true);
+  return run_iter_engine(Y, xview.t, dmrg, rc, max_rank, opts->eps, max_iters, tol, out,
+                         result, op);
+}
+
 static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
                             ttg_tensor* outs, ttg_round_result* results, const char* op)
 {
@@ -1420,6 +1713,13 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
     return fail(TTG_ERR_ARG, std::string(op) + ": bad arguments");
   if (int32_t st = check_opts(opts, op))
     return st;
+  if (opts->method == TTG_METHOD_ALS || opts->method == TTG_METHOD_DMRG)
+  {
+    if (count != 1)
+      return fail(TTG_ERR_METHOD, std::string(op) + ": ALS / DMRG are served for one tensor "
+                                                    "at a time (ttg_round, ttg_round_iter)");
+    return round_iter_impl(ins, opts, nullptr, false, outs, results, op);
+  }
   if (opts->method != TTG_METHOD_SVD && opts->method != TTG_METHOD_SKETCH)
     return fail(TTG_ERR_METHOD, std::string(op) +
                                     ": round_method::svd_streaming / svd_naive are only valid on "
@@ -1753,6 +2053,50 @@ static int32_t apply_round_common(const ttg_tensor* a, const ttg_tensor* x,
   return TTG_OK;
 }
 
+// matvec/matmat ALS and DMRG rounding (round/tt_matvec_als_round.hpp,
+// tt_matvec_dmrg_round.hpp, tt_matmat_als_round.hpp, tt_matmat_dmrg_round.hpp):
+// the raw product on the device, then the iterative rounder started from a
+// random TT (the SVD round when ALS has no max_rank).
+static int32_t apply_round_iter(const ttg_tensor* A, const ttg_tensor* x,
+                                const ttg_round_options* opts, const ttg_iter_options* it,
+                                ttg_tensor* out, ttg_round_result* result, bool matmat,
+                                const char* op)
+{
+  if (!out)
+    return fail(TTG_ERR_ARG, std::string(op) + ": null output");
+  OwnedTensor prod;
+  if (int32_t st = apply_round_common(A, x, nullptr, &prod.t, nullptr, matmat, 0, op))
+    return st;
+  return round_iter_impl(&prod.t, opts, it, true, out, result, op);
+}
+
+int32_t ttg_round_iter(const ttg_tensor* in, const ttg_round_options* opts,
+                       const ttg_iter_options* iter, ttg_tensor* out, ttg_round_result* result)
+{
+  g_err.clear();
+  if (!out)
+    return fail(TTG_ERR_ARG, "round_iter: null output");
+  if (int32_t st = check_opts(opts, "round_iter"))
+    return st;
+  if (opts->method != TTG_METHOD_ALS && opts->method != TTG_METHOD_DMRG)
+    return fail(TTG_ERR_METHOD, "round_iter: method must be als or dmrg");
+  return round_iter_impl(in, opts, iter, false, out, result, "round_iter");
+}
+
+int32_t ttg_apply_round_iter(const ttg_tensor* A, const ttg_tensor* x,
+                             const ttg_round_options* opts, const ttg_iter_options* iter,
+                             ttg_tensor* out, ttg_round_result* result)
+{
+  g_err.clear();
+  if (!A || !x)
+    return fail(TTG_ERR_ARG, "apply_round_iter: null tensor");
+  if (int32_t st = check_opts(opts, "apply_round_iter"))
+    return st;
+  if (opts->method != TTG_METHOD_ALS && opts->method != TTG_METHOD_DMRG)
+    return fail(TTG_ERR_METHOD, "apply_round_iter: method must be als or dmrg");
+  return apply_round_iter(A, x, opts, iter, out, result, x->cols != nullptr, "apply_round_iter");
+}
+
 int32_t ttg_matvec_round(const ttg_tensor* A, const ttg_tensor* x, const ttg_round_options* opts,
                          ttg_tensor* out, ttg_round_result* result)
 {
@@ -1765,6 +2109,8 @@ int32_t ttg_matvec_round(const ttg_tensor* A, const ttg_tensor* x, const ttg_rou
     return fail(TTG_ERR_METHOD, "matvec_round: the sketch method serves round() only");
   if (opts->gauge != TTG_GAUGE_NONE)
     return fail(TTG_ERR_ARG, "matvec_round: gauge is a round() option");
+  if (opts->method == TTG_METHOD_ALS || opts->method == TTG_METHOD_DMRG)
+    return apply_round_iter(A, x, opts, nullptr, out, result, false, "matvec_round");
   const bool streaming = opts->method == TTG_METHOD_SVD_STREAMING && A && A->d > 1;
   return apply_round_common(A, x, opts, out, result, false, streaming ? 2 : 1, "matvec_round");
 }
@@ -1781,6 +2127,8 @@ int32_t ttg_matmat_round(const ttg_tensor* A, const ttg_tensor* B, const ttg_rou
     return fail(TTG_ERR_METHOD, "matmat_round: the sketch method serves round() only");
   if (opts->gauge != TTG_GAUGE_NONE)
     return fail(TTG_ERR_ARG, "matmat_round: gauge is a round() option");
+  if (opts->method == TTG_METHOD_ALS || opts->method == TTG_METHOD_DMRG)
+    return apply_round_iter(A, B, opts, nullptr, out, result, true, "matmat_round");
   const bool streaming = opts->method == TTG_METHOD_SVD && A && A->d > 1;
   return apply_round_common(A, B, opts, out, result, true, streaming ? 2 : 1, "matmat_round");
 }

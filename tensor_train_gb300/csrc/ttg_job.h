@@ -90,6 +90,12 @@ struct TTInfo
   int32_t sketch_state;  // 0 exact round, 1 sketch accepted, 2 sketch rejected -> exact
   int32_t pad;
   double sketch_err;     // ||X - Y|| / ||X|| of the sketch projection
+  // Iterative rounding (kJobAls / kJobDmrg), on the start TT's record:
+  int32_t iters_run;     // sweeps pairs run
+  int32_t iter_conv;     // 1 when the change fell to tol
+  double final_change;   // last max relative change of the bond spectra
+  int64_t env_off;       // arena offset of the item's environments and spectra
+  int64_t env_stride;    // doubles per environment matrix (>= max X rank * max Y rank)
 };
 
 // Per-bond record written by the exact rounder when RoundJob::bond_stats is
@@ -114,6 +120,8 @@ enum JobKind : int32_t
   kJobRoundSketch = 5,    // randomised sketch rounding with an exact check and fallback
   kJobSoftThreshold = 6,  // right_orthogonalize, then R->L singular-value soft thresholding
   kJobLeftOrth = 7,       // left_orthogonalize only (the L->R QR sweep)
+  kJobAls = 8,            // ALS rounding of TT a_idx[i] into the start TT b_idx[i]
+  kJobDmrg = 9,           // two-site DMRG rounding, same pairing
 };
 
 // Grid barrier word of the whole-GPU kernel (zeroed before each launch).
@@ -207,7 +215,42 @@ struct RoundJob
   const double* pristine_arena;
   const CoreSlot* pristine_slots;
   BondStat* bond_stats;  // optional per-bond spectrum summary of the exact rounder
+  // Iterative rounding: sweep-pair limit, convergence tolerance on the
+  // change of the bond spectra, and whether the start TT is already
+  // right-orthogonal (round_right_canonical cold start).
+  int32_t max_iters;
+  int32_t x_right_canonical;
+  double tol;
 };
+
+// Scratch of one CTA for ALS / DMRG on a TT with Y's dims (ry, n) and the
+// start TT's bond capacities (cx): environments, local updates, QR steps,
+// merged pairs and their SVDs.
+TTG_HD inline int64_t need_iter(int d, const int* ry, const int* n, const int* cx, bool dmrg)
+{
+  int64_t need = 64;
+  for (int k = 0; k < d; ++k)
+  {
+    const int64_t yr = ry[k], yrp = ry[k + 1], nk = n[k], xr = cx[k], xrp = cx[k + 1];
+    const int64_t big = (yr > xr ? yr : xr) * (yrp > xrp ? yrp : xrp) * nk;
+    int64_t t = 3 * a32(big) + a32(yr * xr) + a32(yrp * xrp);
+    const int64_t hp = k > 0 ? static_cast<int64_t>(cx[k - 1]) * n[k - 1] : 0;
+    const int64_t wn = k + 1 < d ? static_cast<int64_t>(n[k + 1]) * cx[k + 2] : 0;
+    t = imax64(t, need_left_qr(xr * nk, xrp, wn));
+    t = imax64(t, need_right_qr(xr, nk * xrp, hp));
+    t = imax64(t, need_left_svd(xr * nk, xrp) + a32(xr * nk * xrp));
+    if (dmrg && k + 1 < d)
+    {
+      const int64_t n1 = n[k + 1], yr2 = ry[k + 2], xr2 = cx[k + 2];
+      const int64_t rows = xr * nk, cols = n1 * xr2;
+      const int64_t m = a32(xr * nk * yrp) + a32(yrp * n1 * xr2) + a32(rows * cols);
+      t = imax64(t, m + need_left_svd(rows, cols) + need_left_svd(cols, rows));
+      (void)yr2;
+    }
+    need = imax64(need, t);
+  }
+  return need + 64;
+}
 
 // Scratch of the sketch phase of one TT (inner-product chain, stored right
 // environments, one L->R sketch step); the deterministic round that follows

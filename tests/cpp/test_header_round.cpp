@@ -63,6 +63,30 @@ int main()
     CHECK(tt::norm(tt::sub(a, ar)) <= 0.01 * tt::norm(a) * 1.01, "round error bound");
   }
   {
+    // ALS and DMRG through round_options (test_tt_round.cpp's iterative
+    // cases): a rank-8 sum rounded back to its exact rank.
+    auto a = tt::random({3, 4, 3, 4}, 4, 5), b = tt::random({3, 4, 3, 4}, 4, 6);
+    auto s = tt::add(a, b);
+    const int rmax = 8;
+    for (tt::round_method m : {tt::round_method::als, tt::round_method::dmrg})
+    {
+      tt::round_options it;
+      it.method = m;
+      it.eps = m == tt::round_method::dmrg ? 1e-12 : 0.0;
+      it.max_rank = rmax;
+      it.max_iters = 3;
+      tt::round_result info;
+      auto y = tt::round(s, it, &info);
+      CHECK(frob_diff(y.to_dense(), s.to_dense()) <= 1e-10 * frob(s.to_dense()),
+            "als/dmrg round keeps the tensor");
+      CHECK(info.iters_run >= 1 && info.iters_run <= 3, "als/dmrg iters_run");
+      it.warm_start_tt = &y;
+      auto y2 = tt::round(s, it, &info);
+      CHECK(frob_diff(y2.to_dense(), s.to_dense()) <= 1e-10 * frob(s.to_dense()),
+            "als/dmrg warm start");
+    }
+  }
+  {
     auto A = tt::random(std::vector<int>{2, 3, 2, 3}, std::vector<int>{3, 2, 3, 2}, 3, 0xAA11ULL);
     auto x = tt::random({3, 2, 3, 2}, 3, 0xBB22ULL);
     tt::round_options s = o;
