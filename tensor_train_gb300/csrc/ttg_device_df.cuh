@@ -478,26 +478,27 @@ __device__ __noinline__ int cta_jacobi(E* A, int m, int n, int64_t lda, E* V, in
 // truncate_eps_rank, types/tt_eigen_bridge.hpp:172-197, with no max_rank
 // cap below c).  Then the SVD only rotates a basis: U diag(s) V^T = Q R gives
 // the same represented tensor and the same rank whether the left factor is U
-// and diag(s) V^T is absorbed, or Q and R.  This routine proves that case
+// and diag(s) V^T is absorbed, or Q and R.  These routines prove that case
 // from the R factor of the step's QR, so the Jacobi SVD can be skipped.
 //
 // Test: R^T R - tau I is positive definite, shown by an LDL^T elimination
 // that meets only positive pivots.  tau covers every rounding error between
-// the bond matrix X and the computed pivots:
-//   * sigma_min(X) >= sigma_min(R) - e_R with e_R = c h u ||R||_F, a bound on
-//     the backward error of the Householder QR that produced R (Higham,
-//     Accuracy and Stability of Numerical Algorithms, 2nd ed., thm. 19.4,
-//     with the constant taken generously);
-//   * forming R^T R and eliminating it perturb its eigenvalues by at most
-//     2 (c + 1)^2 u ||R||_F^2 (thms. 3.5 and 10.3 there, normwise);
-// so positive pivots with tau = (delta + e_R)^2 + 2 (c + 1)^2 u ||R||_F^2
-// imply sigma_min(X) > delta.  u is the unit roundoff of the arithmetic
-// (2^-53 for FP64; 2^-47 for df64, below its 48-bit significand).  A NaN
-// anywhere fails the test (the comparison with a NaN pivot is false), and
-// the caller then runs the SVD, which reports it.
-//
-// R: c x c upper triangular, column-major (ld c).  G: c x c scratch of
-// E-sized elements (lower triangle used).  h: rows of the step's matrix.
+// the bond matrix X and the computed pivots (u = unit roundoff of the
+// arithmetic, gamma_n = n u / (1 - n u); Higham, Accuracy and Stability of
+// Numerical Algorithms, 2nd ed.):
+//   * sigma_min(X) >= sigma_min(R) - e_R, e_R = c h u_QR ||R||_F, a bound on
+//     the backward error of the Householder QR that produced R (thm. 19.4,
+//     constant taken generously);
+//   * fl(R^T R) = R^T R + E1 with ||E1||_2 <= gamma_c ||R||_F^2 (inner
+//     products of length <= c; || |R|^T |R| ||_F <= ||R||_F^2);
+//   * an LDL^T elimination with positive pivots factors fl(R^T R) - tau I +
+//     E2 with |E2| <= gamma_{c+1} |L||D||L^T| (thm. 10.3), and
+//     || |L||D||L^T| ||_F <= trace(L D L^T) <= (1 + gamma_c) ||R||_F^2;
+// so positive pivots with tau = (1 + 4u)(delta + e_R)^2 + 4 (c + 1) u
+// ||R||_F^2 imply sigma_min(X) > delta.  u is 2^-53 for FP64 and 2^-44 for
+// df64 (its operations are accurate to a few units of 2^-48: Joldes, Muller
+// & Popescu, ACM TOMS 2017).  A NaN anywhere fails the test (a comparison
+// with a NaN pivot is false) and the caller runs the SVD, which reports it.
 // ---------------------------------------------------------------------------
 template <class E>
 struct CertOps;
@@ -520,13 +521,68 @@ struct CertOps<df64>
   static __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return df_fma(a, b, c); }
   static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
   static __device__ __forceinline__ df64 neg(df64 a) { return df_neg(a); }
-  static __device__ __forceinline__ df64 sub(df64 a, df64 b) { return df_sub(a, b); }
-  static constexpr double u = 7.105427357601002e-15;  // 2^-47
+  static __device__ __forceinline__ df64 sub(df64 a, double b) { return df_sub(a, df_from(b)); }
+  static constexpr double u = 5.684341886080802e-14;  // 2^-44
 };
 
+// The shift tau (see above) for R / s with ||R / s||_F^2 = fro2, the
+// threshold dl = delta / s, arithmetic unit roundoff u and QR unit roundoff uqr.
+__device__ __forceinline__ double certify_tau(double dl, double fro2, int c, int h, double u,
+                                              double uqr)
+{
+  const double eR = static_cast<double>(c) * h * uqr * sqrt(fro2);
+  return (1.0 + 4.0 * u) * (dl + eR) * (dl + eR) + 4.0 * (c + 1.0) * u * fro2;
+}
+
+// (i, j), i >= j, of entry t of a lower triangle packed by rows.
+__device__ __forceinline__ void tri_index(int64_t t, int* i_out, int* j_out)
+{
+  int i = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+  while (static_cast<int64_t>(i) * (i + 1) / 2 > t)
+    --i;
+  while (static_cast<int64_t>(i + 1) * (i + 2) / 2 <= t)
+    ++i;
+  *i_out = i;
+  *j_out = static_cast<int>(t - static_cast<int64_t>(i) * (i + 1) / 2);
+}
+
+// LDL^T elimination of the lower triangle of G (c x c, column-major, ld c),
+// in place; true when every pivot is positive.  Only the pivots are needed:
+// G(i, k) -= G(i, j) G(k, j) / G(j, j) for j < k <= i.
+template <class E>
+__device__ bool cta_ldl_positive(E* G, int c)
+{
+  using O = CertOps<E>;
+  for (int j = 0; j < c; ++j)
+  {
+    const double piv = O::to(G[j + static_cast<int64_t>(j) * c]);
+    if (!(piv > 0.0))
+      return false;  // every thread reads the same pivot: a uniform exit
+    if (j == c - 1)
+      break;
+    const E inv = O::from(1.0 / piv);
+    const int rem = c - 1 - j;  // trailing order
+    const int64_t ntr = static_cast<int64_t>(rem) * (rem + 1) / 2;
+    const E* gj = G + static_cast<int64_t>(j) * c;
+    for (int64_t t = threadIdx.x; t < ntr; t += blockDim.x)
+    {
+      int a, b;
+      tri_index(t, &a, &b);
+      const int i = j + 1 + a, k = j + 1 + b;  // i >= k > j
+      E& g = G[i + static_cast<int64_t>(k) * c];
+      g = O::fma(O::neg(O::mul(gj[i], inv)), gj[k], g);
+    }
+    __syncthreads();
+  }
+  return true;
+}
+
+// R: c x c upper triangular, column-major (ld c).  G: c x c scratch of
+// E-sized elements (lower triangle used).  h: rows of the step's matrix;
+// uqr: unit roundoff of the QR that produced R.
 template <class E>
 __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, int h, double delta,
-                                                       E* G, CtaShared& sh)
+                                                       E* G, CtaShared& sh, double uqr)
 {
   using O = CertOps<E>;
   if (c < 1)
@@ -545,58 +601,55 @@ __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, i
   const double fro2 = cta_sum(part, sh);  // ||R / s||_F^2
   if (!(fro2 > 0.0) || !isfinite(fro2))
     return false;
-  const double dl = delta * is;
-  const double eR = static_cast<double>(c) * h * O::u * sqrt(fro2);
-  const double tau = (dl + eR) * (dl + eR) + 2.0 * (c + 1.0) * (c + 1.0) * O::u * fro2;
+  const double tau = certify_tau(delta * is, fro2, c, h, O::u, uqr);
   // G = (R/s)^T (R/s) - tau I, lower triangle: G(i, j) = sum_{p <= j} R(p, i) R(p, j).
   const int64_t ntri = static_cast<int64_t>(c) * (c + 1) / 2;
   for (int64_t t = threadIdx.x; t < ntri; t += blockDim.x)
   {
-    // t -> (i, j), i >= j, packed by rows of the lower triangle.
-    int i = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
-    while (static_cast<int64_t>(i) * (i + 1) / 2 > t)
-      --i;
-    while (static_cast<int64_t>(i + 1) * (i + 2) / 2 <= t)
-      ++i;
-    const int j = static_cast<int>(t - static_cast<int64_t>(i) * (i + 1) / 2);
+    int i, j;
+    tri_index(t, &i, &j);
     const double* ri = R + static_cast<int64_t>(i) * c;
     const double* rj = R + static_cast<int64_t>(j) * c;
     E acc = O::from(0.0);
     for (int p = 0; p <= j; ++p)
       acc = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), acc);
     if (i == j)
-      acc = O::sub(acc, O::from(tau));
+      acc = O::sub(acc, tau);
     G[i + static_cast<int64_t>(j) * c] = acc;
   }
   __syncthreads();
-  // LDL^T elimination of the lower triangle (the pivots are all that is
-  // needed): G(i, k) -= G(i, j) G(k, j) / G(j, j) for j < k <= i.
-  for (int j = 0; j < c; ++j)
+  return cta_ldl_positive<E>(G, c);
+}
+
+// The same test with G = R^T R already formed in FP64 (lower triangle
+// used; the whole-GPU sweep forms it over the grid): G is scaled by 1/s^2
+// and shifted in place, then eliminated in FP64 by this CTA.
+__device__ __noinline__ bool cta_certify_from_gram(double* G, const double* R, int c, int h,
+                                                   double delta, CtaShared& sh, double uqr)
+{
+  if (c < 1)
+    return false;
+  const double s = cta_pow2_of_max(View{R, 1, c}, c, c, sh);
+  const double is = 1.0 / s;
+  const int64_t cc = static_cast<int64_t>(c) * c;
+  double part = 0.0;
+  for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
   {
-    const double piv = O::to(G[j + static_cast<int64_t>(j) * c]);
-    if (!(piv > 0.0))
-      return false;  // every thread reads the same pivot: a uniform exit
-    if (j == c - 1)
-      break;
-    const E inv = O::from(1.0 / piv);
-    const int rem = c - 1 - j;  // trailing order
-    const int64_t ntr = static_cast<int64_t>(rem) * (rem + 1) / 2;
-    const E* gj = G + static_cast<int64_t>(j) * c;
-    for (int64_t t = threadIdx.x; t < ntr; t += blockDim.x)
-    {
-      int a = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
-      while (static_cast<int64_t>(a) * (a + 1) / 2 > t)
-        --a;
-      while (static_cast<int64_t>(a + 1) * (a + 2) / 2 <= t)
-        ++a;
-      const int b = static_cast<int>(t - static_cast<int64_t>(a) * (a + 1) / 2);
-      const int i = j + 1 + a, k = j + 1 + b;  // i >= k > j
-      E& g = G[i + static_cast<int64_t>(k) * c];
-      g = O::fma(O::neg(O::mul(gj[i], inv)), gj[k], g);
-    }
-    __syncthreads();
+    const double x = R[t] * is;
+    part += x * x;
   }
-  return true;
+  const double fro2 = cta_sum(part, sh);
+  if (!(fro2 > 0.0) || !isfinite(fro2))
+    return false;
+  const double tau = certify_tau(delta * is, fro2, c, h, CertOps<double>::u, uqr);
+  for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+  {
+    const int64_t i = t % c, j = t / c;
+    if (i >= j)
+      G[t] = G[t] * is * is - (i == j ? tau : 0.0);
+  }
+  __syncthreads();
+  return cta_ldl_positive<double>(G, c);
 }
 
 // ---------------------------------------------------------------------------

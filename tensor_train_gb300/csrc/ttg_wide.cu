@@ -119,10 +119,14 @@ __device__ void wide_copy(const WideJob& job, double* dst, const double* src, in
 // on the tensor cores (FP64-accurate, oz_tile) when the job allows them and
 // K <= 512, else 64x64 FP64 tiles.  Returns false if a tensor-core wait
 // timed out (the grid error word is set).
+// fp64_only: FP64 tiles even when the sliced tensor-core tiles are on
+// (products whose error bound is stated for FP64).
 __device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View B, double* C,
-                          int64_t c_rs, int64_t c_cs, WideSmem sm, CtaShared& sh)
+                          int64_t c_rs, int64_t c_cs, WideSmem sm, CtaShared& sh,
+                          bool fp64_only = false)
 {
-  if (job.tc && sm.oz && K <= 512 && static_cast<int64_t>(kOzSmemBytes) <= sm.cap * 8)
+  if (!fp64_only && job.tc && sm.oz && K <= 512 &&
+      static_cast<int64_t>(kOzSmemBytes) <= sm.cap * 8)
   {
     const int tm = (M + kOzM - 1) / kOzM, tn = (N + kOzN - 1) / kOzN;
     bool ok = true;
@@ -664,40 +668,85 @@ __device__ bool wide_left_svd(const WideJob& job, View X, int h, int c, double d
   const int nsv = h < c ? h : c;
   const double floor2 = 1e-6 * delta * delta / static_cast<double>(nsv > 1 ? nsv : 1);
   int sweeps = 0, conv = 1, r_new = 1;
-  if (h >= 2 * c)
+  // No-truncation certificate (cta_certify_from_gram) as in the per-TT
+  // left_svd: tried when no bond statistics are asked for and max_rank
+  // cannot cut below c; for h >= c the step then takes the QR route.
+  const bool certify = bs == nullptr && h >= c && c >= 2 &&
+                       (job.max_rank <= 0 || job.max_rank >= c);
+  if (h >= 2 * c || certify)
   {
     bool ok = true;
     wide_qr(job, X, h, c, sm, sh, &ok);
     if (!ok)
       return false;
-    // A = R (c x c), then Jacobi.
-    wide_copy(job, job.A, job.R, static_cast<int64_t>(c) * c);
-    WSYNC();
-    if (job.mixed)
+    bool certified = false;
+    if (certify)
     {
-      if (!wide_svd_mixed(job, View{job.R, 1, c}, c, c, false, floor2, sm, sh, &sweeps, &conv))
+      // G = R^T R (FP64) over the grid into job.A, then one CTA eliminates
+      // it (FP64) and proves sigma_min(R) > delta; the decision reaches every
+      // CTA through job.ival[1].  The QR here is FP64 on both paths.
+      if (!wide_gemm(job, c, c, c, View{job.R, c, 1}, View{job.R, 1, c}, job.A, 1, c, sm, sh,
+                     true))
         return false;
+      WSYNC();
+      if (me == 0)
+      {
+        const bool yes =
+          cta_certify_from_gram(job.A, job.R, c, h, delta, sh, CertOps<double>::u);
+        if (threadIdx.x == 0)
+          job.ival[1] = yes ? 1 : 0;
+      }
+      WSYNC();
+      certified = *reinterpret_cast<volatile const int*>(job.ival + 1) != 0;
     }
-    else if (!wide_jacobi<double>(job, job.A, c, c, c, nullptr, job.jblock, floor2,
-                                  kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
-      return false;
-    if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
-      return false;
-    r_new = job.ival[0];
-    // Uc (c x r_new) = A(:, ord) / s, into V.
-    for (int j = me; j < r_new; j += job.size)
+    if (certified)
     {
-      const double s = job.sorted[j];
-      const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
-      for (int i = threadIdx.x; i < c; i += blockDim.x)
-        job.V[i + static_cast<int64_t>(j) * c] = s > 0.0 ? a[i] / s : 0.0;
+      // Every singular value is kept: U = Q (Uc = I in V), F = R.
+      r_new = c;
+      const int64_t cc = static_cast<int64_t>(c) * c;
+      for (int64_t e = job.rank * static_cast<int64_t>(blockDim.x) + threadIdx.x; e < cc;
+           e += static_cast<int64_t>(job.size) * blockDim.x)
+      {
+        const int64_t i = e % c, j = e / c;
+        job.V[e] = i == j ? 1.0 : 0.0;
+        job.F[i * c + j] = job.R[e];
+      }
+      WSYNC();
+      wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
+      WSYNC();
     }
-    WSYNC();
-    // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
-    if (!wide_gemm(job, r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sm, sh))
-      return false;
-    wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
-    WSYNC();
+    else
+    {
+      // A = R (c x c), then Jacobi.
+      wide_copy(job, job.A, job.R, static_cast<int64_t>(c) * c);
+      WSYNC();
+      if (job.mixed)
+      {
+        if (!wide_svd_mixed(job, View{job.R, 1, c}, c, c, false, floor2, sm, sh, &sweeps, &conv))
+          return false;
+      }
+      else if (!wide_jacobi<double>(job, job.A, c, c, c, nullptr, job.jblock, floor2,
+                                    kJacobiStopRel, job.max_sweeps, sm, sh, &sweeps, &conv))
+        return false;
+      if (!wide_truncate(job, job.A, c, c, c, delta, T, bs, sh))
+        return false;
+      r_new = job.ival[0];
+      // Uc (c x r_new) = A(:, ord) / s, into V.
+      for (int j = me; j < r_new; j += job.size)
+      {
+        const double s = job.sorted[j];
+        const double* a = job.A + static_cast<int64_t>(job.ord[j]) * c;
+        for (int i = threadIdx.x; i < c; i += blockDim.x)
+          job.V[i + static_cast<int64_t>(j) * c] = s > 0.0 ? a[i] / s : 0.0;
+      }
+      WSYNC();
+      // F = Uc^T R (r_new x c, row-major); U = Q [Uc; 0] (h x r_new).
+      if (!wide_gemm(job, r_new, c, c, View{job.V, c, 1}, View{job.R, 1, c}, job.F, c, 1, sm,
+                     sh))
+        return false;
+      wide_apply_q(job, h, c, job.V, c, r_new, job.Ub, 1, h, false, sm, sh);
+      WSYNC();
+    }
   }
   else if (h >= c)
   {
