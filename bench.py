@@ -74,6 +74,10 @@ def parse():
     ap.add_argument("--cpu-sample", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--only", choices=["both", "mixed", "fp64"], default="both",
+                    help="batch workload: time one precision only (profiling cases)")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="keep the plan's default launch configuration (profiling cases)")
     ap.add_argument("--workload", default="batch",
                     choices=["batch", "round_d10", "matvec_d20", "round_d40", "eval_d32",
                              "sketch_d64"],
@@ -238,7 +242,7 @@ def run_ours(args):
         torch.cuda.synchronize()
         # Launch configuration by the plan's autotuner, then one CUDA graph
         # per step (deep copy from the pristine inputs + the sweep launch).
-        tuned = plan.autotune(sptr)
+        tuned = "default" if args.no_autotune else plan.autotune(sptr)
         plan.graph(True)
         for _ in range(args.warmup):
             plan.run(sptr)
@@ -279,6 +283,16 @@ def run_ours(args):
                 "ms_step": ms_step, "value": count * world / (ms_step / 1e3),
                 "kernel_ms": statistics.mean(kms), "clocks": clocks, "io": io}
 
+    if args.only != "both":
+        # One precision, no CPU legs: a short case for profilers.
+        r = measure(T.precision[args.only])
+        print(json.dumps({"workload": f"batch of {count}", "precision": args.only,
+                          "ms_per_step": r["ms_step"], "kernel_ms": r["kernel_ms"],
+                          "value": r["value"], "autotune": r["tuned"],
+                          "device_status_errors": r["bad"]}), flush=True)
+        if world > 1:
+            torch.distributed.destroy_process_group()
+        return
     plain = measure(T.precision.fp64)
     mixed = measure(T.precision.mixed)
     opts = mixed["opts"]
@@ -496,7 +510,7 @@ def run_single(args):
     def timed(plan, tune=False):
         plan.upload(sptr)
         if tune:  # launch configuration by the autotuner, then CUDA-graph replays
-            plan.tuned = plan.autotune(sptr)
+            plan.tuned = "default" if args.no_autotune else plan.autotune(sptr)
             plan.graph(True)
         for _ in range(args.warmup):
             plan.run(sptr)
