@@ -1,6 +1,7 @@
 // tcgen05 (5th-generation tensor core) building blocks for sm_103a, written
 // as inline PTX: TMEM allocation, single-thread MMA issue with operands in
-// shared memory, completion through an mbarrier, TMEM -> register loads.
+// shared memory, completion through an mbarrier, TMEM -> register loads, and
+// TMA (cp.async.bulk.tensor) copies into the 128-byte swizzled layout.
 //
 // Operand layout: K-major, no swizzle ("interleaved" canonical layout).  A
 // tile of R rows x K columns of 16-bit elements is stored as 8x8 core
@@ -113,6 +114,39 @@ __device__ __forceinline__ bool mbar_wait(uint64_t* mbar, uint32_t parity, uint3
       return true;
   }
   return false;
+}
+
+// Single thread: arrive on the mbarrier and add `bytes` to the transaction
+// count that the TMA copies signalling it must complete.
+__device__ __forceinline__ void mbar_arrive_expect_tx(uint64_t* mbar, uint32_t bytes)
+{
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(mbar)),
+               "r"(bytes)
+               : "memory");
+}
+
+// Single thread: TMA copy of the box at (x, y) of a 2-D tensor map into
+// shared memory; completion is signalled on the mbarrier (complete_tx).
+// x * element size must be a multiple of 16 bytes.
+__device__ __forceinline__ void tma_load_2d(void* dst, const void* tmap, uint64_t* mbar, int x,
+                                            int y)
+{
+  asm volatile(
+    "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%3, "
+    "%4}], [%2];" ::"r"(smem_u32(dst)),
+    "l"(reinterpret_cast<uint64_t>(tmap)), "r"(smem_u32(mbar)), "r"(x), "r"(y)
+    : "memory");
+}
+
+// Shared-memory matrix descriptor for a K-major tile in the 128-byte
+// swizzled layout that a TMA copy with 128-byte swizzle writes: rows of
+// 64 BF16 (128 bytes), 8-row atoms of 1024 bytes (SBO), layout type 2
+// (128B swizzle) in [61,64), version 1; the tile base 1024-byte aligned.
+// A K step of 16 elements inside the atom advances the start by 32 bytes.
+__device__ __forceinline__ uint64_t smem_desc_sw128(uint32_t saddr)
+{
+  return static_cast<uint64_t>((saddr >> 4) & 0x3FFF) | (1ull << 16) |
+         (static_cast<uint64_t>(1024 >> 4) << 32) | (1ull << 46) | (2ull << 61);
 }
 
 // Generic-proxy shared-memory writes become visible to the tensor core.
