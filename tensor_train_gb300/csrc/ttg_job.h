@@ -42,7 +42,7 @@ TTG_HD inline int64_t need_right_qr(int64_t r, int64_t w, int64_t h_prev)
 // left_qr_step on a core (h = r*n, rp) with next core of w_next columns.
 TTG_HD inline int64_t need_left_qr(int64_t h, int64_t rp, int64_t w_next)
 {
-  return 2 * a32(h * rp) + a32(rp) + a32(rp * rp) + a32(rp * w_next);
+  return a32(h * rp) + a32(rp) + a32(rp * rp) + a32(rp * w_next);
 }
 TTG_HD inline int64_t need_svd_step(int64_t h, int64_t c, int64_t w_next)
 {

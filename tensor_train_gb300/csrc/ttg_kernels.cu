@@ -22,7 +22,6 @@
 #include "ttg_job.h"
 #include "ttg_kernels.h"
 #include "ttg_sweep_common.cuh"
-#include "ttg_wy.cuh"
 
 namespace ttg
 {
@@ -53,17 +52,14 @@ __device__ void gemm_sel(bool mixed, int M, int N, int K, View A, View B, double
 // Dynamic shared memory of the CTA, used to stage the matrix a step works
 // on when it fits (cap doubles).
 
-// QR of X (h x c), blocked Householder (ttg_wy.cuh).  Q -> Qg (h x k,
-// column-major, ld h; *Qout = Qg), R -> R (k x c, column-major, ld k),
-// k = min(h, c).  The factorisation runs in shared memory when h*c fits
-// there, else in Wg.  X is read before Qg is written, so Qg may be X's
-// memory.
+// QR of X (h x c).  Q -> *W (h x k, column-major, ld h), R -> R (k x c,
+// column-major, ld k), k = min(h, c).  The factorisation runs in shared
+// memory when h*c fits there, else in Wg; *W tells the caller where Q is.
 __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* R, Smem sm,
-                         double* Qg, double** Qout, bool mixed, CtaShared& sh)
+                         double** Wout, bool mixed, CtaShared& sh)
 {
   double* W = (static_cast<int64_t>(h) * c <= sm.cap) ? sm.p : Wg;
-  *Qout = Qg;
-  const int k = h < c ? h : c;
+  *Wout = W;
   if (mixed)
   {
     // df64 factorisation of X / 2^e; R scaled back exactly; Q rounded to FP64.
@@ -72,23 +68,24 @@ __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* 
     const double s = cta_pow2_of_max(X, h, c, sh);
     cta_split_to_df(Wd, h, X, h, c, 1.0 / s);
     __syncthreads();
-    cta_qr_wy<df64>(Wd, h, c, h, td, sh);
+    cta_householder_qr_df(Wd, h, c, h, td, sh);
+    const int k = h < c ? h : c;
     cta_extract_r_df(R, Wd, k, c, h, s);
-    df64* Qd = reinterpret_cast<df64*>(Qg);
-    cta_form_q_wy<df64>(Wd, h, k, h, td, Qd, h, sh);
+    cta_form_q_df(Wd, h, k, h, td);
     for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * k; t += blockDim.x)
     {
-      const df64 q = Qd[t];
-      Qg[t] = df_to(q);
+      const df64 q = Wd[t];
+      W[t] = df_to(q);
     }
     __syncthreads();
     return k;
   }
   cta_copy_to_colmajor(W, h, X, h, c);
   __syncthreads();
-  cta_qr_wy<double>(W, h, c, h, tau, sh);
+  cta_householder_qr(W, h, c, h, tau, sh);
+  const int k = h < c ? h : c;
   cta_extract_r(R, W, k, c, h);
-  cta_form_q_wy<double>(W, h, k, h, tau, Qg, h, sh);
+  cta_form_q(W, h, k, h, tau);
   return k;
 }
 
@@ -152,14 +149,14 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       const double sX = cta_pow2_of_max(X, h, c, sh);
       cta_split_to_df(Wd, h, X, h, c, 1.0 / sX);
       __syncthreads();
-      cta_qr_wy<df64>(Wd, h, c, h, td, sh);
+      cta_householder_qr_df(Wd, h, c, h, td, sh);
       cta_extract_r_df(R, Wd, c, c, h, sX);
     }
     else
     {
       cta_copy_to_colmajor(W, h, X, h, c);
       __syncthreads();
-      cta_qr_wy<double>(W, h, c, h, tau, sh);
+      cta_householder_qr(W, h, c, h, tau, sh);
       cta_extract_r(R, W, c, c, h);
     }
     const bool certified =
@@ -223,7 +220,7 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
         Ud[t] = i < c ? df_from(Uc[i + static_cast<int64_t>(jj) * c]) : df64{0.0f, 0.0f};
       }
       __syncthreads();
-      cta_apply_q_wy<df64>(Wd, h, c, h, td, Ud, r_new, h, sh);
+      cta_apply_q_df(Wd, h, c, h, td, Ud, r_new, h);
       for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
       {
         const df64 u = Ud[t];
@@ -239,7 +236,7 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
         U[t] = i < c ? Uc[i + static_cast<int64_t>(jj) * c] : 0.0;
       }
       __syncthreads();
-      cta_apply_q_wy<double>(W, h, c, h, tau, U, r_new, h, sh);
+      cta_apply_q(W, h, c, h, tau, U, r_new, h);
     }
     if (!certified)
       record_bond(bs, sorted, c, r_new);
@@ -415,12 +412,11 @@ __device__ __noinline__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& 
   double* R = bump.take(static_cast<int64_t>(r) * r);
   double* P = bump.take(static_cast<int64_t>(hp) * r);
   double* Q;
-  // Q (w x k, column-major) is formed straight into the core's slot: as a
-  // row-major (k x w) block it is the new right_unfold(cur).
-  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sm, cs, &Q, mixed, sh);
+  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sm, &Q, mixed, sh);
   // prev (hp x k) = left_unfold(prev) (hp x r) * L, L(a, e) = R(e, a).
   gemm_sel(mixed, hp, k, r, View{ps, r, 1}, View{R, k, 1}, P, k, 1, sh);
   cta_copy(ps, P, static_cast<int64_t>(hp) * k);
+  cta_copy(cs, Q, static_cast<int64_t>(w) * k);
   set_ranks(cur, k, rp);
   set_ranks(prev, prev.r, k);
   __syncthreads();
@@ -440,8 +436,7 @@ __device__ __noinline__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& n
   double* R = bump.take(static_cast<int64_t>(rp) * rp);
   double* P = bump.take(static_cast<int64_t>(rp) * wn);
   double* Q;
-  double* Qg = bump.take(static_cast<int64_t>(h) * rp);
-  const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sm, Qg, &Q, mixed, sh);
+  const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sm, &Q, mixed, sh);
   // next (k x wn) = R (k x rp) * right_unfold(next) (rp x wn).
   gemm_sel(mixed, k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, P, wn, 1, sh);
   cta_copy(ns, P, static_cast<int64_t>(k) * wn);
@@ -893,8 +888,7 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
     double* tau = b2.take(l);
     double* Rq = b2.take(static_cast<int64_t>(l) * l);
     double* Q;
-    const int lq = qr_factor(View{Z, 1, h}, h, l, Wq, tau, Rq, Smem{nullptr, 0}, Z, &Q, mixed,
-                             sh);
+    const int lq = qr_factor(View{Z, 1, h}, h, l, Wq, tau, Rq, Smem{nullptr, 0}, &Q, mixed, sh);
     // M (lq x rp) = Q^T left_unfold(cur).
     double* M = b2.take(static_cast<int64_t>(lq) * rp);
     gemm_sel(mixed, lq, rp, h, View{Q, h, 1}, View{ar + cur.off, rp, 1}, M, rp, 1, sh);
