@@ -31,6 +31,9 @@ METRIC = ("TT roundings/sec and matvec_round/sec at rel. err<=1e-8: mixed/learne
           "FP64, 1 GB300")
 EPS = 1e-8
 SEED0 = 1000
+# DRAM bytes (read + write) of one mixed round_kernel launch on TTs 1000..1607
+# of the batch at 4 CTAs per SM (ncu, profiles/round_kernel_batch608_ncu.md).
+TRAFFIC_608 = 7.988859392e9 + 20.41651968e9
 
 
 def measured_peaks(path=None):
@@ -340,12 +343,18 @@ def run_ours(args):
         "data": "synthetic: seeded uneven random TTs (mt19937_64 + normal_distribution)",
         "config": workload_config(count),
         "precision": "mixed", "parallelism": f"{world} independent shard(s), one GPU each",
-        # traffic: DRAM read+write bytes of one mixed round_kernel launch from an
-        # ncu capture of a 304-TT slice of this batch (4.567 GB), scaled to 4096
-        # TTs by the TT count; per-CTA scratch spill, not input bytes.
-        "roofline": roofline_tensor(flops, kernel_ms, peak, traffic=4.567e9 * count / 304,
+        # traffic: DRAM read + write bytes of one mixed round_kernel launch at
+        # the benched 4 CTAs per SM, from the ncu capture of a 608-TT slice of
+        # this batch (7.989 GB read + 20.417 GB written), scaled to `count`
+        # TTs by the TT count; it is per-CTA scratch of the work matrices
+        # evicted from L2, set against the algorithmic bytes (input cores read,
+        # output cores written).
+        "roofline": roofline_tensor(flops, kernel_ms, peak, traffic=TRAFFIC_608 * count / 608,
                                     kernel="round_kernel (precision=mixed)",
-                                    flop_model="algorithmic F_round (tensor_train_gb300/flops.py)"),
+                                    flop_model="algorithmic F_round (tensor_train_gb300/flops.py)",
+                                    algorithmic_bytes=sum(mixed["io"]),
+                                    traffic_over_algorithmic=TRAFFIC_608 * count / 608 /
+                                    max(sum(mixed["io"]), 1)),
         "plain_fp64": {"value": plain["value"], "ms_per_step": plain["ms_step"],
                        "kernel_ms": plain["kernel_ms"], "achieved_tflops": plain_achieved,
                        "frac": plain_achieved / peak, "clocks": plain["clocks"],

@@ -1226,7 +1226,11 @@ int32_t ttg_plan_autotune(ttg_plan* P, void* stream, int32_t* choice)
       }
     if (P->wide_teams_max <= 1)
     {
-      for (int tcv = 0; tcv <= P->wjob.mixed; ++tcv)
+      // The sliced-BF16 tensor-core tiles are tried only when they were
+      // opted into (TTG_WIDE_TENSOR_CORES=1): they are no faster on these
+      // barrier-bound sweeps and carry ~1e-12 instead of FP64 rounding per
+      // product, which reached 2.6e-10 on the d=40 rank-257 round.
+      for (int tcv = 0; tcv <= (P->wjob.mixed && P->wjob.tc ? 1 : 0); ++tcv)
         for (int b : {2, 4, 8})
           if ((6 * c_max + 2) * b <= kSmemOnePerSm)
             cands.push_back({100 + b + 1000 * tcv, true, P->wide_grid, kSmemOnePerSm, b, tcv, 1, 1});
