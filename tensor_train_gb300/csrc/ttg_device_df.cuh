@@ -522,7 +522,6 @@ struct CertOps<double>
   static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
   static __device__ __forceinline__ double neg(double a) { return -a; }
   static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
-  static __device__ __forceinline__ double add(double a, double b) { return a + b; }
   static constexpr double u = 1.1102230246251565e-16;  // 2^-53
 };
 template <>
@@ -534,7 +533,6 @@ struct CertOps<df64>
   static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
   static __device__ __forceinline__ df64 neg(df64 a) { return df_neg(a); }
   static __device__ __forceinline__ df64 sub(df64 a, double b) { return df_sub(a, df_from(b)); }
-  static __device__ __forceinline__ df64 add(df64 a, df64 b) { return df_add(a, b); }
   static constexpr double u = 5.684341886080802e-14;  // 2^-44
 };
 
@@ -623,19 +621,9 @@ __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, i
     tri_index(t, &i, &j);
     const double* ri = R + static_cast<int64_t>(i) * c;
     const double* rj = R + static_cast<int64_t>(j) * c;
-    // four independent partial sums (shorter dependency chains)
-    E a0 = O::from(0.0), a1 = a0, a2 = a0, a3 = a0;
-    int p = 0;
-    for (; p + 3 <= j; p += 4)
-    {
-      a0 = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), a0);
-      a1 = O::fma(O::from(ri[p + 1] * is), O::from(rj[p + 1] * is), a1);
-      a2 = O::fma(O::from(ri[p + 2] * is), O::from(rj[p + 2] * is), a2);
-      a3 = O::fma(O::from(ri[p + 3] * is), O::from(rj[p + 3] * is), a3);
-    }
-    for (; p <= j; ++p)
-      a0 = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), a0);
-    E acc = O::add(O::add(a0, a1), O::add(a2, a3));
+    E acc = O::from(0.0);
+    for (int p = 0; p <= j; ++p)
+      acc = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), acc);
     if (i == j)
       acc = O::sub(acc, tau);
     G[i + static_cast<int64_t>(j) * c] = acc;
