@@ -115,24 +115,6 @@ __device__ void cta_copy_to_rowmajor(double* dst, int64_t ld, View src, int64_t 
   }
 }
 
-// Dot of a reflector v (v[0] = 1 implicit) with y over [0, len), by one
-// warp: four independent partial sums per lane, then the warp sum.
-__device__ __forceinline__ double warp_dot_unit(const double* v, const double* y, int len, int lane)
-{
-  double d0 = (lane == 0) ? y[0] : 0.0, d1 = 0.0, d2 = 0.0, d3 = 0.0;
-  int i = 1 + lane;
-  for (; i + 96 < len; i += 128)
-  {
-    d0 = fma(v[i], y[i], d0);
-    d1 = fma(v[i + 32], y[i + 32], d1);
-    d2 = fma(v[i + 64], y[i + 64], d2);
-    d3 = fma(v[i + 96], y[i + 96], d3);
-  }
-  for (; i < len; i += 32)
-    d0 = fma(v[i], y[i], d0);
-  return warp_sum((d0 + d1) + (d2 + d3));
-}
-
 // ---------------------------------------------------------------------------
 // Householder QR, in place.  A column-major (m x c, ld).  On return the
 // upper triangle of the leading (k x c) block holds R (k = min(m, c)), the
@@ -182,7 +164,10 @@ __device__ __noinline__ void cta_householder_qr(double* A, int m, int c, int64_t
       for (int col = j + 1 + w; col < c; col += kWarps)
       {
         double* y = A + col * ld + j;
-        const double dot = warp_dot_unit(x, y, len, lane) * t;
+        double dot = 0.0;
+        for (int i = lane; i < len; i += 32)
+          dot += (i == 0 ? 1.0 : x[i]) * y[i];
+        dot = warp_sum(dot) * t;
         for (int i = lane; i < len; i += 32)
           y[i] -= dot * (i == 0 ? 1.0 : x[i]);
       }
@@ -219,7 +204,10 @@ __device__ __noinline__ void cta_form_q(double* A, int m, int k, int64_t ld, con
       for (int col = j + 1 + w; col < k; col += kWarps)
       {
         double* y = A + col * ld + j;
-        const double dot = warp_dot_unit(v, y, len, lane) * t;
+        double dot = 0.0;
+        for (int i = lane; i < len; i += 32)
+          dot += (i == 0 ? 1.0 : v[i]) * y[i];
+        dot = warp_sum(dot) * t;
         for (int i = lane; i < len; i += 32)
           y[i] -= dot * (i == 0 ? 1.0 : v[i]);
       }
@@ -250,7 +238,10 @@ __device__ __noinline__ void cta_apply_q(const double* A, int m, int kref, int64
     for (int col = w; col < p; col += kWarps)
     {
       double* y = B + col * ldb + j;
-      const double dot = warp_dot_unit(v, y, len, lane) * t;
+      double dot = 0.0;
+      for (int i = lane; i < len; i += 32)
+        dot += (i == 0 ? 1.0 : v[i]) * y[i];
+      dot = warp_sum(dot) * t;
       for (int i = lane; i < len; i += 32)
         y[i] -= dot * (i == 0 ? 1.0 : v[i]);
     }

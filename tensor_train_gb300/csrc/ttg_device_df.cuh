@@ -80,26 +80,6 @@ __device__ void cta_split_to_df(df64* W, int64_t ld, View X, int64_t m, int64_t 
   }
 }
 
-// Dot of a reflector v (v[0] = 1 implicit) with y over [0, len), by one
-// warp: four independent partial sums per lane (a df64 FMA is a long
-// dependency chain), then the warp sum.
-__device__ __forceinline__ df64 warp_dot_unit_df(const df64* v, const df64* y, int len, int lane)
-{
-  const df64 z{0.0f, 0.0f};
-  df64 d0 = (lane == 0) ? y[0] : z, d1 = z, d2 = z, d3 = z;
-  int i = 1 + lane;
-  for (; i + 96 < len; i += 128)
-  {
-    d0 = df_fma(v[i], y[i], d0);
-    d1 = df_fma(v[i + 32], y[i + 32], d1);
-    d2 = df_fma(v[i + 64], y[i + 64], d2);
-    d3 = df_fma(v[i + 96], y[i + 96], d3);
-  }
-  for (; i < len; i += 32)
-    d0 = df_fma(v[i], y[i], d0);
-  return df_warp_sum(df_add(df_add(d0, d1), df_add(d2, d3)));
-}
-
 // Householder QR in df64, in place (see cta_householder_qr for the layout
 // and convention).  tau is kept in df64.
 __device__ __noinline__ void cta_householder_qr_df(df64* A, int m, int c, int64_t ld, df64* tau, CtaShared& sh)
@@ -146,7 +126,10 @@ __device__ __noinline__ void cta_householder_qr_df(df64* A, int m, int c, int64_
       for (int col = j + 1 + w; col < c; col += kWarps)
       {
         df64* y = A + col * ld + j;
-        const df64 dot = df_mul(warp_dot_unit_df(x, y, len, lane), td);
+        df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
+        for (int i = 1 + lane; i < len; i += 32)
+          dot = df_fma(x[i], y[i], dot);
+        dot = df_mul(df_warp_sum(dot), td);
         const df64 nd = df_neg(dot);
         if (lane == 0)
           y[0] = df_add(y[0], nd);
@@ -184,7 +167,10 @@ __device__ __noinline__ void cta_form_q_df(df64* A, int m, int k, int64_t ld, co
       for (int col = j + 1 + w; col < k; col += kWarps)
       {
         df64* y = A + col * ld + j;
-        const df64 dot = df_mul(warp_dot_unit_df(v, y, len, lane), t);
+        df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
+        for (int i = 1 + lane; i < len; i += 32)
+          dot = df_fma(v[i], y[i], dot);
+        dot = df_mul(df_warp_sum(dot), t);
         const df64 nd = df_neg(dot);
         if (lane == 0)
           y[0] = df_add(y[0], nd);
@@ -219,7 +205,10 @@ __device__ __noinline__ void cta_apply_q_df(const df64* A, int m, int kref, int6
     for (int col = w; col < p; col += kWarps)
     {
       df64* y = B + col * ldb + j;
-      const df64 dot = df_mul(warp_dot_unit_df(v, y, len, lane), t);
+      df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
+      for (int i = 1 + lane; i < len; i += 32)
+        dot = df_fma(v[i], y[i], dot);
+      dot = df_mul(df_warp_sum(dot), t);
       const df64 nd = df_neg(dot);
       if (lane == 0)
         y[0] = df_add(y[0], nd);
