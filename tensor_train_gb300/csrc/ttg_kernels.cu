@@ -210,8 +210,26 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       // F = Uc^T R  (= diag(s) V^T restricted to the kept rows).
       gemm_sel(mixed, r_new, c, c, View{Uc, c, 1}, View{R, 1, c}, F, c, 1, sh);
     }
-    // U = Q [Uc; 0] by applying the reflectors.
-    if (mixed)
+    // U = Q [Uc; 0] by applying the reflectors.  A certified bond keeps
+    // every column (Uc = I): U is Q itself, formed in place from the
+    // reflectors (dorg2r order, which skips the zero structure of [I; 0]).
+    if (certified)
+    {
+      if (mixed)
+      {
+        cta_form_q_df(Wd, h, c, h, td);
+        for (int64_t t = threadIdx.x; t < hc; t += blockDim.x)
+        {
+          const df64 q = Wd[t];
+          W[t] = df_to(q);
+        }
+        __syncthreads();
+      }
+      else
+        cta_form_q(W, h, c, h, tau);
+      U = W;
+    }
+    else if (mixed)
     {
       df64* Ud = reinterpret_cast<df64*>(U);
       for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
