@@ -786,9 +786,11 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
     for (int i = 0; i < count; ++i)
     {
       const Shape& sh = P.shapes[i];
-      int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1;
+      int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1, gsum = 0;
       for (int k = 0; k < sh.d; ++k)
       {
+        if (k >= 1)
+          gsum += static_cast<int64_t>(sh.r[k]) * sh.r[k];
         rmax = std::max<int64_t>(rmax, std::max(sh.r[k], sh.r[k + 1]));
         hmax = std::max<int64_t>(hmax, static_cast<int64_t>(sh.r[k]) * sh.mode(k));
         nmax = std::max<int64_t>(nmax, sh.mode(k));
@@ -804,7 +806,7 @@ int32_t build_round_plan(ttg_plan& P, int32_t count, const ttg_tensor* ins,
         }
       }
       pos += sh.d > 0 ? sh.d - 1 : 0;
-      need = std::max(need, need_sketch(rmax, lsum, lmax, hmax, nmax) + 64);
+      need = std::max(need, need_sketch(rmax, lsum, lmax, hmax, nmax, gsum) + 64);
     }
   }
   std::stable_sort(cost.begin(), cost.end(),

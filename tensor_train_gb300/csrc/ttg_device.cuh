@@ -46,6 +46,9 @@ struct CtaShared
   int item;
   int ival[4];
   double dval[4];
+  double hh[4];       // Householder scalars broadcast by thread 0 (FP64 QR)
+  double ldl_inv[2];  // inverse of the next LDL^T pivot, double-buffered
+  int ldl_ok[2];      // that pivot is positive
 };
 
 template <class T>
@@ -122,56 +125,88 @@ __device__ void cta_copy_to_rowmajor(double* dst, int64_t ld, View src, int64_t 
 // implicit) and tau[j] its scale: H_j = I - tau_j v_j v_j^T.  Reflector
 // convention of Eigen's makeHouseholder (beta = -sign(x0)*||x||; an exactly
 // zero tail gives tau = 0), as in qr_thin (types/tt_eigen_bridge.hpp:42-60).
+// Thread 0 alone forms the reflector scalars (one FP64 square root and two
+// divisions) and broadcasts t and 1 / (x0 - beta); the trailing update uses
+// the unscaled column with that factor folded in, and the column's own
+// scaling to v is deferred to the next reflector's norm pass.
 // ---------------------------------------------------------------------------
 __device__ __noinline__ void cta_householder_qr(double* A, int m, int c, int64_t ld, double* tau, CtaShared& sh)
 {
   const int k = m < c ? m : c;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  double inv_prev = 0.0;
   for (int j = 0; j < k; ++j)
   {
     double* x = A + j * ld + j;
     const int len = m - j;
+    if (j > 0)
+    {
+      double* xp = x - ld - 1;  // column j - 1 from its diagonal
+      for (int i = 1 + threadIdx.x; i <= len; i += blockDim.x)
+        xp[i] *= inv_prev;
+    }
     double part = 0.0;
     for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
-      part += x[i] * x[i];
-    const double tail2 = cta_sum(part, sh);
-    const double x0 = x[0];
-    double beta, t, inv;
-    if (tail2 <= DBL_MIN)
-    {
-      t = 0.0;
-      beta = x0;
-      inv = 0.0;
-    }
-    else
-    {
-      beta = sqrt(x0 * x0 + tail2);
-      if (x0 >= 0.0)
-        beta = -beta;
-      inv = 1.0 / (x0 - beta);
-      t = (beta - x0) / beta;
-    }
-    for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
-      x[i] *= inv;
+      part = fma(x[i], x[i], part);
+    part = warp_sum(part);
+    if (lane == 0)
+      sh.red[w] = part;
     __syncthreads();
     if (threadIdx.x == 0)
     {
+      double tail2 = 0.0;
+#pragma unroll
+      for (int i = 0; i < kWarps; ++i)
+        tail2 += sh.red[i];
+      const double x0 = x[0];
+      double beta, t, inv;
+      if (tail2 <= DBL_MIN)
+      {
+        t = 0.0;
+        beta = x0;
+        inv = 0.0;
+      }
+      else
+      {
+        beta = sqrt(x0 * x0 + tail2);
+        if (x0 >= 0.0)
+          beta = -beta;
+        inv = 1.0 / (x0 - beta);
+        t = (beta - x0) / beta;
+      }
       x[0] = beta;
       tau[j] = t;
+      sh.hh[0] = t;
+      sh.hh[1] = inv;
     }
+    __syncthreads();
+    const double t = sh.hh[0], inv = sh.hh[1];
     if (t != 0.0)
     {
       for (int col = j + 1 + w; col < c; col += kWarps)
       {
         double* y = A + col * ld + j;
         double dot = 0.0;
-        for (int i = lane; i < len; i += 32)
-          dot += (i == 0 ? 1.0 : x[i]) * y[i];
-        dot = warp_sum(dot) * t;
-        for (int i = lane; i < len; i += 32)
-          y[i] -= dot * (i == 0 ? 1.0 : x[i]);
+        for (int i = 1 + lane; i < len; i += 32)
+          dot = fma(x[i], y[i], dot);
+        // t (y0 + v1..^T y1..), v = x * inv: lane 0 alone reads and writes y0.
+        const double y0 = (lane == 0) ? y[0] : 0.0;
+        dot = warp_sum(fma(dot, inv, y0)) * t;
+        const double nd = -dot * inv;
+        if (lane == 0)
+          y[0] = y0 - dot;
+        for (int i = 1 + lane; i < len; i += 32)
+          y[i] = fma(nd, x[i], y[i]);
       }
     }
+    inv_prev = inv;
+    __syncthreads();
+  }
+  if (k > 0)
+  {
+    double* xl = A + (k - 1) * ld + (k - 1);
+    for (int i = 1 + threadIdx.x; i < m - (k - 1); i += blockDim.x)
+      xl[i] *= inv_prev;
     __syncthreads();
   }
 }

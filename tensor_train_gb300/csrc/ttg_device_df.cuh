@@ -69,86 +69,130 @@ __device__ double cta_pow2_of_max(View X, int64_t m, int64_t n, CtaShared& sh)
   return __longlong_as_double(static_cast<long long>(ex) << 52);
 }
 
-// W (df64, column-major m x n, ld) = split(X / scale).
-__device__ void cta_split_to_df(df64* W, int64_t ld, View X, int64_t m, int64_t n, double inv_scale)
+// W (df64, column-major m x n, ld) = split(X * 2^k).
+__device__ void cta_split_to_df(df64* W, int64_t ld, View X, int64_t m, int64_t n, int k)
 {
   const int64_t total = m * n;
   for (int64_t t = threadIdx.x; t < total; t += blockDim.x)
   {
     const int64_t i = t % m, j = t / m;
-    W[i + j * ld] = df_from(X(i, j) * inv_scale);
+    W[i + j * ld] = df_split_pow2(X(i, j), k);
   }
 }
 
+// W[t] (FP64) = A[t] (df64) for t < n, in place when W and A alias
+// element for element.
+__device__ void cta_join_from_df(double* W, const df64* A, int64_t n)
+{
+  for (int64_t t = threadIdx.x; t < n; t += blockDim.x)
+  {
+    const df64 a = A[t];
+    W[t] = df_join_pow2(a, 0);
+  }
+  __syncthreads();
+}
+
+// The reflector of x = (x0, x1..) with ||x1..||^2 = tail2, in df64 on the
+// FP32 pipes: H = I - t v v^T, v = (1, x1.. * inv), H x = (beta, 0..);
+// t = 0 (no reflection) when the tail is negligible.
+__device__ __forceinline__ void householder_scalars_df(df64 x0, df64 tail2, df64* beta, df64* t,
+                                                       df64* inv)
+{
+  if (tail2.hi <= 1.0e-36f)
+  {
+    *beta = x0;
+    *t = df64{0.0f, 0.0f};
+    *inv = df64{0.0f, 0.0f};
+    return;
+  }
+  df64 b = df_sqrt(df_fma(x0, x0, tail2));
+  if (x0.hi >= 0.0f)
+    b = df_neg(b);
+  const df64 den = df_sub(x0, b);  // x0 and beta have opposite signs: no cancellation
+  *beta = b;
+  *inv = df_recip(den);
+  *t = df_neg(df_mul(den, df_recip(b)));  // (beta - x0) / beta
+}
+
 // Householder QR in df64, in place (see cta_householder_qr for the layout
-// and convention).  tau is kept in df64.
+// and convention).  tau is kept in df64.  Every thread forms the reflector
+// scalars itself from the warp partial sums (FP32 pipes, no broadcast), the
+// trailing update uses the unscaled column with inv folded in, and the
+// column's own scaling to v is deferred to the next reflector's norm pass:
+// two barriers per reflector.
 __device__ __noinline__ void cta_householder_qr_df(df64* A, int m, int c, int64_t ld, df64* tau, CtaShared& sh)
 {
   const int k = m < c ? m : c;
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  df64* red = reinterpret_cast<df64*>(sh.red);
+  df64 inv_prev{0.0f, 0.0f};
   for (int j = 0; j < k; ++j)
   {
     df64* x = A + j * ld + j;
     const int len = m - j;
+    if (j > 0)
+    {
+      df64* xp = x - ld - 1;  // column j - 1 from its diagonal
+      for (int i = 1 + threadIdx.x; i <= len; i += blockDim.x)
+        xp[i] = df_mul(xp[i], inv_prev);
+    }
     df64 part{0.0f, 0.0f};
     for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
       part = df_fma(x[i], x[i], part);
-    const double tail2 = df_to(cta_sum_df(part, sh));
-    const df64 x0d = x[0];
-    const double x0 = df_to(x0d);
-    double beta, t, inv;
-    if (tail2 <= 1.0e-36)
-    {
-      t = 0.0;
-      beta = x0;
-      inv = 0.0;
-    }
-    else
-    {
-      beta = sqrt(x0 * x0 + tail2);
-      if (x0 >= 0.0)
-        beta = -beta;
-      inv = 1.0 / (x0 - beta);
-      t = (beta - x0) / beta;
-    }
-    const df64 invd = df_from(inv);
-    for (int i = 1 + threadIdx.x; i < len; i += blockDim.x)
-      x[i] = (t == 0.0) ? df64{0.0f, 0.0f} : df_mul(x[i], invd);
+    part = df_warp_sum(part);
+    const df64 x0 = x[0];
+    if (lane == 0)
+      red[w] = part;
     __syncthreads();
-    const df64 td = df_from(t);
+    df64 tail2{0.0f, 0.0f};
+#pragma unroll
+    for (int i = 0; i < kWarps; ++i)
+      tail2 = df_add(tail2, red[i]);
+    df64 beta, td, inv;
+    householder_scalars_df(x0, tail2, &beta, &td, &inv);
     if (threadIdx.x == 0)
     {
-      x[0] = df_from(beta);
+      x[0] = beta;
       tau[j] = td;
     }
-    if (t != 0.0)
+    if (td.hi != 0.0f)
     {
       for (int col = j + 1 + w; col < c; col += kWarps)
       {
         df64* y = A + col * ld + j;
-        df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
+        df64 dot{0.0f, 0.0f};
         for (int i = 1 + lane; i < len; i += 32)
           dot = df_fma(x[i], y[i], dot);
-        dot = df_mul(df_warp_sum(dot), td);
-        const df64 nd = df_neg(dot);
+        // t (y0 + v1..^T y1..), v = x * inv: lane 0 alone reads and writes y0.
+        const df64 y0 = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
+        dot = df_mul(df_warp_sum(df_fma(dot, inv, y0)), td);
+        const df64 nd = df_neg(df_mul(dot, inv));
         if (lane == 0)
-          y[0] = df_add(y[0], nd);
+          y[0] = df_sub(y0, dot);
         for (int i = 1 + lane; i < len; i += 32)
           y[i] = df_fma(nd, x[i], y[i]);
       }
     }
+    inv_prev = inv;
+    __syncthreads();
+  }
+  if (k > 0)
+  {
+    df64* xl = A + (k - 1) * ld + (k - 1);
+    for (int i = 1 + threadIdx.x; i < m - (k - 1); i += blockDim.x)
+      xl[i] = df_mul(xl[i], inv_prev);
     __syncthreads();
   }
 }
 
-// R (k x c, column-major, FP64, ld k) = upper triangle of A, times scale.
-__device__ void cta_extract_r_df(double* R, const df64* A, int k, int c, int64_t ld, double scale)
+// R (k x c, column-major, FP64, ld k) = upper triangle of A, times 2^e.
+__device__ void cta_extract_r_df(double* R, const df64* A, int k, int c, int64_t ld, int e)
 {
   const int64_t total = static_cast<int64_t>(k) * c;
   for (int64_t t = threadIdx.x; t < total; t += blockDim.x)
   {
     const int i = static_cast<int>(t % k), j = static_cast<int>(t / k);
-    R[t] = (i <= j) ? df_to(A[i + j * ld]) * scale : 0.0;
+    R[t] = (i <= j) ? df_join_pow2(A[i + j * ld], e) : 0.0;
   }
   __syncthreads();
 }
@@ -506,22 +550,25 @@ template <>
 struct CertOps<double>
 {
   static __device__ __forceinline__ double from(double x) { return x; }
-  static __device__ __forceinline__ double to(double x) { return x; }
   static __device__ __forceinline__ double fma(double a, double b, double c) { return ::fma(a, b, c); }
   static __device__ __forceinline__ double mul(double a, double b) { return a * b; }
   static __device__ __forceinline__ double neg(double a) { return -a; }
   static __device__ __forceinline__ double sub(double a, double b) { return a - b; }
+  static __device__ __forceinline__ double recip(double a) { return 1.0 / a; }
+  static __device__ __forceinline__ bool positive(double a) { return a > 0.0; }
   static constexpr double u = 1.1102230246251565e-16;  // 2^-53
 };
 template <>
 struct CertOps<df64>
 {
-  static __device__ __forceinline__ df64 from(double x) { return df_from(x); }
-  static __device__ __forceinline__ double to(df64 x) { return df_to(x); }
+  static __device__ __forceinline__ df64 from(double x) { return df_split_pow2(x, 0); }
   static __device__ __forceinline__ df64 fma(df64 a, df64 b, df64 c) { return df_fma(a, b, c); }
   static __device__ __forceinline__ df64 mul(df64 a, df64 b) { return df_mul(a, b); }
   static __device__ __forceinline__ df64 neg(df64 a) { return df_neg(a); }
-  static __device__ __forceinline__ df64 sub(df64 a, double b) { return df_sub(a, df_from(b)); }
+  static __device__ __forceinline__ df64 sub(df64 a, df64 b) { return df_sub(a, b); }
+  static __device__ __forceinline__ df64 recip(df64 a) { return df_recip(a); }
+  // hi carries the sign of a normalised pair; NaN compares false.
+  static __device__ __forceinline__ bool positive(df64 a) { return a.hi > 0.0f; }
   static constexpr double u = 5.684341886080802e-14;  // 2^-44
 };
 
@@ -534,10 +581,12 @@ __device__ __forceinline__ double certify_tau(double dl, double fro2, int c, int
   return (1.0 + 4.0 * u) * (dl + eR) * (dl + eR) + 4.0 * (c + 1.0) * u * fro2;
 }
 
-// (i, j), i >= j, of entry t of a lower triangle packed by rows.
+// (i, j), i >= j, of entry t of a lower triangle packed by rows.  The FP32
+// square root lands within one of i for t < 2^21 (8t + 1 exact in FP32);
+// the integer steps settle it, and any t.
 __device__ __forceinline__ void tri_index(int64_t t, int* i_out, int* j_out)
 {
-  int i = static_cast<int>((sqrt(8.0 * static_cast<double>(t) + 1.0) - 1.0) * 0.5);
+  int i = static_cast<int>((sqrtf(8.0f * static_cast<float>(t) + 1.0f) - 1.0f) * 0.5f);
   while (static_cast<int64_t>(i) * (i + 1) / 2 > t)
     --i;
   while (static_cast<int64_t>(i + 1) * (i + 2) / 2 <= t)
@@ -546,49 +595,67 @@ __device__ __forceinline__ void tri_index(int64_t t, int* i_out, int* j_out)
   *j_out = static_cast<int>(t - static_cast<int64_t>(i) * (i + 1) / 2);
 }
 
-// LDL^T elimination of the lower triangle of G (c x c, column-major, ld c),
-// in place; true when every pivot is positive.  Only the pivots are needed:
-// G(i, k) -= G(i, j) G(k, j) / G(j, j) for j < k <= i.
+// LDL^T elimination of G - shift I (G: lower triangle of a c x c matrix,
+// column-major, ld c, eliminated in place without its shift); true when
+// every pivot is positive.  Only the pivots are needed: G(i, k) -= G(i, j)
+// G(k, j) / (G(j, j) - shift) for j < k <= i.  The diagonal is stored
+// unshifted (the updates are linear, so the shift enters the pivots only).
+// Thread 0 owns entry (j+1, j+1) of every trailing update, so it finishes
+// the next pivot, tests it and broadcasts its inverse through shared memory
+// (double-buffered by step parity): one barrier per step, and the FP64
+// division of the plain path runs on one thread instead of all of them.
 template <class E>
-__device__ bool cta_ldl_positive(E* G, int c)
+__device__ bool cta_ldl_positive(E* G, int c, E shift, CtaShared& sh)
 {
   using O = CertOps<E>;
+  static_assert(sizeof(E) == sizeof(double), "pivot slots hold 8-byte elements");
+  E* inv_buf = reinterpret_cast<E*>(sh.ldl_inv);
+  if (threadIdx.x == 0)
+  {
+    const E piv = O::sub(G[0], shift);
+    sh.ldl_ok[0] = O::positive(piv) ? 1 : 0;
+    inv_buf[0] = O::recip(piv);
+  }
+  __syncthreads();
   for (int j = 0; j < c; ++j)
   {
-    const double piv = O::to(G[j + static_cast<int64_t>(j) * c]);
-    if (!(piv > 0.0))
-      return false;  // every thread reads the same pivot: a uniform exit
+    const int b = j & 1;
+    if (!sh.ldl_ok[b])
+      return false;  // every thread reads the same flag: a uniform exit
     if (j == c - 1)
       break;
-    const E inv = O::from(1.0 / piv);
+    const E inv = inv_buf[b];
     const int rem = c - 1 - j;  // trailing order
     const int64_t ntr = static_cast<int64_t>(rem) * (rem + 1) / 2;
     const E* gj = G + static_cast<int64_t>(j) * c;
     for (int64_t t = threadIdx.x; t < ntr; t += blockDim.x)
     {
-      int a, b;
-      tri_index(t, &a, &b);
-      const int i = j + 1 + a, k = j + 1 + b;  // i >= k > j
+      int a, bb;
+      tri_index(t, &a, &bb);
+      const int i = j + 1 + a, k = j + 1 + bb;  // i >= k > j
       E& g = G[i + static_cast<int64_t>(k) * c];
       g = O::fma(O::neg(O::mul(gj[i], inv)), gj[k], g);
+      if (t == 0)
+      {
+        const E piv = O::sub(g, shift);
+        sh.ldl_ok[b ^ 1] = O::positive(piv) ? 1 : 0;
+        inv_buf[b ^ 1] = O::recip(piv);
+      }
     }
     __syncthreads();
   }
   return true;
 }
 
-// R: c x c upper triangular, column-major (ld c).  G: c x c scratch of
-// E-sized elements (lower triangle used).  h: rows of the step's matrix;
-// uqr: unit roundoff of the QR that produced R.
-template <class E>
+// R: c x c upper triangular, column-major (ld c), FP64.  G: c x c FP64
+// scratch (lower triangle used).  h: rows of the step's matrix; uqr: unit
+// roundoff of the QR that produced R.  The plain path's test.
 __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, int h, double delta,
-                                                       E* G, CtaShared& sh, double uqr)
+                                                       double* G, CtaShared& sh, double uqr)
 {
-  using O = CertOps<E>;
   if (c < 1)
     return false;
-  // Scale by a power of two (exact) so that max |R| is ~1: keeps the
-  // squares inside the FP32 exponent range of df64.
+  // Scale by a power of two (exact) so that max |R| is ~1.
   const double s = cta_pow2_of_max(View{R, 1, c}, c, c, sh);
   const double is = 1.0 / s;
   const int64_t cc = static_cast<int64_t>(c) * c;
@@ -596,13 +663,12 @@ __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, i
   for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
   {
     const double x = R[t] * is;
-    part += x * x;
+    part = fma(x, x, part);
   }
   const double fro2 = cta_sum(part, sh);  // ||R / s||_F^2
   if (!(fro2 > 0.0) || !isfinite(fro2))
     return false;
-  const double tau = certify_tau(delta * is, fro2, c, h, O::u, uqr);
-  // G = (R/s)^T (R/s) - tau I, lower triangle: G(i, j) = sum_{p <= j} R(p, i) R(p, j).
+  // G = (R/s)^T (R/s), lower triangle: G(i, j) = sum_{p <= j} R(p, i) R(p, j) / s^2.
   const int64_t ntri = static_cast<int64_t>(c) * (c + 1) / 2;
   for (int64_t t = threadIdx.x; t < ntri; t += blockDim.x)
   {
@@ -610,20 +676,67 @@ __device__ __noinline__ bool cta_certify_no_truncation(const double* R, int c, i
     tri_index(t, &i, &j);
     const double* ri = R + static_cast<int64_t>(i) * c;
     const double* rj = R + static_cast<int64_t>(j) * c;
-    E acc = O::from(0.0);
+    double acc = 0.0;
     for (int p = 0; p <= j; ++p)
-      acc = O::fma(O::from(ri[p] * is), O::from(rj[p] * is), acc);
-    if (i == j)
-      acc = O::sub(acc, tau);
+      acc = fma(ri[p], rj[p], acc);
+    G[i + static_cast<int64_t>(j) * c] = acc * is * is;
+  }
+  double shift = 0.0;
+  if (threadIdx.x == 0)
+    shift = certify_tau(delta * is, fro2, c, h, CertOps<double>::u, uqr);
+  __syncthreads();
+  return cta_ldl_positive<double>(G, c, shift, sh);  // only thread 0 reads shift
+}
+
+// The mixed path's test, on the df64 R of its QR as it lies in the
+// factored panel: Rd(i, j) = Rd[i + j ld], i <= j, representing R / 2^e
+// (dl = delta / 2^e).  No conversion: the Gram and the elimination run in
+// df64 on the FP32 pipes; ||R||_F^2 and tau are formed once, by thread 0,
+// in FP64.  The Gram entries stay far inside the FP32 range: the panel was
+// scaled so that its largest entry is in [1, 2), so ||R / 2^e||_F >= 1 and
+// every |Rd| <= sqrt(h c) * 2.
+__device__ __noinline__ bool cta_certify_no_truncation_df(const df64* Rd, int64_t ld, int c, int h,
+                                                          double dl, df64* G, CtaShared& sh,
+                                                          double uqr)
+{
+  if (c < 1)
+    return false;
+  const int64_t cc = static_cast<int64_t>(c) * c;
+  df64 part{0.0f, 0.0f};
+  for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
+  {
+    const int i = static_cast<int>(t % c), j = static_cast<int>(t / c);
+    if (i <= j)
+    {
+      const df64 r = Rd[i + static_cast<int64_t>(j) * ld];
+      part = df_fma(r, r, part);
+    }
+  }
+  const df64 f2 = cta_sum_df(part, sh);
+  if (!(f2.hi > 0.0f) || !(f2.hi < 1.0e30f))
+    return false;  // zero, overflowing or NaN: the SVD path decides (and reports a NaN)
+  const int64_t ntri = static_cast<int64_t>(c) * (c + 1) / 2;
+  for (int64_t t = threadIdx.x; t < ntri; t += blockDim.x)
+  {
+    int i, j;
+    tri_index(t, &i, &j);
+    const df64* ri = Rd + static_cast<int64_t>(i) * ld;
+    const df64* rj = Rd + static_cast<int64_t>(j) * ld;
+    df64 acc{0.0f, 0.0f};
+    for (int p = 0; p <= j; ++p)
+      acc = df_fma(ri[p], rj[p], acc);
     G[i + static_cast<int64_t>(j) * c] = acc;
   }
+  df64 shift{0.0f, 0.0f};
+  if (threadIdx.x == 0)
+    shift = df_split_pow2(certify_tau(dl, df_join_pow2(f2, 0), c, h, CertOps<df64>::u, uqr), 0);
   __syncthreads();
-  return cta_ldl_positive<E>(G, c);
+  return cta_ldl_positive<df64>(G, c, shift, sh);  // only thread 0 reads shift
 }
 
 // The same test with G = R^T R already formed in FP64 (lower triangle
 // used; the whole-GPU sweep forms it over the grid): G is scaled by 1/s^2
-// and shifted in place, then eliminated in FP64 by this CTA.
+// in place, then eliminated in FP64 by this CTA.
 __device__ __noinline__ bool cta_certify_from_gram(double* G, const double* R, int c, int h,
                                                    double delta, CtaShared& sh, double uqr)
 {
@@ -636,20 +749,22 @@ __device__ __noinline__ bool cta_certify_from_gram(double* G, const double* R, i
   for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
   {
     const double x = R[t] * is;
-    part += x * x;
+    part = fma(x, x, part);
   }
   const double fro2 = cta_sum(part, sh);
   if (!(fro2 > 0.0) || !isfinite(fro2))
     return false;
-  const double tau = certify_tau(delta * is, fro2, c, h, CertOps<double>::u, uqr);
   for (int64_t t = threadIdx.x; t < cc; t += blockDim.x)
   {
     const int64_t i = t % c, j = t / c;
     if (i >= j)
-      G[t] = G[t] * is * is - (i == j ? tau : 0.0);
+      G[t] = G[t] * is * is;
   }
+  double shift = 0.0;
+  if (threadIdx.x == 0)
+    shift = certify_tau(delta * is, fro2, c, h, CertOps<double>::u, uqr);
   __syncthreads();
-  return cta_ldl_positive<double>(G, c);
+  return cta_ldl_positive<double>(G, c, shift, sh);
 }
 
 // ---------------------------------------------------------------------------
@@ -712,27 +827,28 @@ __device__ __noinline__ int cta_jacobi_mixed(View src, int m, int n, double* A, 
   // 4. Polish in df64: A / 2^e split once, df64 sweeps, back to FP64.
   const double sc = cta_pow2_of_max(View{A, 1, lda}, m, n, sh);
   const double isc = 1.0 / sc;
+  const int esc = pow2_exponent(sc);
   df64* Ad = reinterpret_cast<df64*>(A);
   for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
   {
     const int64_t e = (t % m) + (t / m) * lda;
-    Ad[e] = df_from(A[e] * isc);
+    Ad[e] = df_split_pow2(A[e], -esc);
   }
   df64* Vdd = reinterpret_cast<df64*>(Vout);
   if (Vout)
     for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-      Vdd[t] = df_from(Vout[t]);
+      Vdd[t] = df_split_pow2(Vout[t], 0);
   __syncthreads();
   const int sweeps = cta_jacobi<df64>(Ad, m, n, lda, Vdd, n, max_sweeps, converged, nrm, sh,
                                       floor2 * isc * isc, kJacobiStopRel);
   for (int64_t t = threadIdx.x; t < mn; t += blockDim.x)
   {
     const int64_t e = (t % m) + (t / m) * lda;
-    A[e] = df_to(Ad[e]) * sc;
+    A[e] = df_join_pow2(Ad[e], esc);
   }
   if (Vout)
     for (int64_t t = threadIdx.x; t < nn; t += blockDim.x)
-      Vout[t] = df_to(Vdd[t]);
+      Vout[t] = df_join_pow2(Vdd[t], 0);
   __syncthreads();
   return sweeps;
 }
@@ -744,9 +860,8 @@ __device__ __noinline__ int cta_jacobi_mixed(View src, int m, int n, double* A, 
 __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
                             int64_t c_cs, CtaShared& sh)
 {
-  const double sa = cta_pow2_of_max(A, M, K, sh);
-  const double sb = cta_pow2_of_max(B, K, N, sh);
-  const double isa = 1.0 / sa, isb = 1.0 / sb, scale = sa * sb;
+  const int ea = pow2_exponent(cta_pow2_of_max(A, M, K, sh));
+  const int eb = pow2_exponent(cta_pow2_of_max(B, K, N, sh));
   df64(*as)[64 + 1] = reinterpret_cast<df64(*)[64 + 1]>(sh.gemm_a);
   df64(*bs)[64 + 1] = reinterpret_cast<df64(*)[64 + 1]>(sh.gemm_b);
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -766,8 +881,8 @@ __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, do
         {
           const int kk = t / 64, ii = t % 64;
           const int gi = i0 + ii, gp = p0 + kk, gj = j0 + ii;
-          as[kk][ii] = (gi < M && gp < K) ? df_from(A(gi, gp) * isa) : df64{0.0f, 0.0f};
-          bs[kk][ii] = (gp < K && gj < N) ? df_from(B(gp, gj) * isb) : df64{0.0f, 0.0f};
+          as[kk][ii] = (gi < M && gp < K) ? df_split_pow2(A(gi, gp), -ea) : df64{0.0f, 0.0f};
+          bs[kk][ii] = (gp < K && gj < N) ? df_split_pow2(B(gp, gj), -eb) : df64{0.0f, 0.0f};
         }
         __syncthreads();
 #pragma unroll 4
@@ -794,7 +909,7 @@ __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, do
         {
           const int gi = i0 + ty + 16 * a, gj = j0 + tx + 16 * b;
           if (gi < M && gj < N)
-            C[gi * c_rs + gj * c_cs] = df_to(acc[a][b]) * scale;
+            C[gi * c_rs + gj * c_cs] = df_join_pow2(acc[a][b], ea + eb);
         }
     }
   __syncthreads();

@@ -257,12 +257,13 @@ TTG_HD inline int64_t need_iter(int d, const int* ry, const int* n, const int* c
 // uses the ordinary round need.  rmax = largest bond rank, lsum = sum over
 // bonds of r_k * l_k, lmax = largest sketch rank, hmax = largest r_k * n_k,
 // nmax = largest mode.
+// gsum: sum of r_k^2 over the bonds k = 1..d-1 (the stored right Grams).
 TTG_HD inline int64_t need_sketch(int64_t rmax, int64_t lsum, int64_t lmax, int64_t hmax,
-                                  int64_t nmax)
+                                  int64_t nmax, int64_t gsum)
 {
-  return 2 * a32(rmax * rmax) + a32(rmax * nmax * rmax) + a32(lsum) + a32(lmax * nmax * lmax) +
+  return a32(gsum) + a32(rmax * nmax * rmax) + a32(1) + a32(lsum) + a32(lmax * nmax * lmax) +
          a32(hmax * lmax) + 3 * a32(hmax * lmax) + a32(lmax) + a32(lmax * lmax) +
-         a32(lmax * rmax) + a32(lmax * nmax * rmax) + 64 * 8;
+         a32(lmax * rmax) + a32(lmax * nmax * rmax) + 2 * a32(hmax * rmax) + 64 * 8;
 }
 
 }  // namespace ttg

@@ -19,6 +19,7 @@
 
 #include "ttg_device.cuh"
 #include "ttg_device_df.cuh"
+#include "ttg_wy_df.cuh"
 #include "ttg_job.h"
 #include "ttg_kernels.h"
 #include "ttg_sweep_common.cuh"
@@ -65,19 +66,25 @@ __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* 
     // df64 factorisation of X / 2^e; R scaled back exactly; Q rounded to FP64.
     df64* Wd = reinterpret_cast<df64*>(W);
     df64* td = reinterpret_cast<df64*>(tau);
-    const double s = cta_pow2_of_max(X, h, c, sh);
-    cta_split_to_df(Wd, h, X, h, c, 1.0 / s);
+    const int e = pow2_exponent(cta_pow2_of_max(X, h, c, sh));
+    cta_split_to_df(Wd, h, X, h, c, -e);
     __syncthreads();
-    cta_householder_qr_df(Wd, h, c, h, td, sh);
     const int k = h < c ? h : c;
-    cta_extract_r_df(R, Wd, k, c, h, s);
-    cta_form_q_df(Wd, h, k, h, td);
-    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * k; t += blockDim.x)
-    {
-      const df64 q = Wd[t];
-      W[t] = df_to(q);
-    }
-    __syncthreads();
+    // A panel in global memory is factored in blocks of kWyB reflectors
+    // with the shared region as staging (it holds nothing else here).
+    const bool wy = W != sm.p && c > kWyB && wy_stage_need(h) <= sm.cap;
+    df64* stage = reinterpret_cast<df64*>(sm.p);
+    df64* T = reinterpret_cast<df64*>(&sh.gemm_b[0][0]);
+    if (wy)
+      cta_householder_qr_df_wy(Wd, h, c, h, td, stage, T, sh);
+    else
+      cta_householder_qr_df(Wd, h, c, h, td, sh);
+    cta_extract_r_df(R, Wd, k, c, h, e);
+    if (wy)
+      cta_form_q_df_wy(Wd, h, k, h, td, stage, T);
+    else
+      cta_form_q_df(Wd, h, k, h, td);
+    cta_join_from_df(W, Wd, static_cast<int64_t>(h) * k);
     return k;
   }
   cta_copy_to_colmajor(W, h, X, h, c);
@@ -144,13 +151,23 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
     const bool A_in_smem = (A == sm.p);
     df64* Wd = reinterpret_cast<df64*>(W);
     df64* td = reinterpret_cast<df64*>(tau);
+    int eX = 0;  // mixed: the panel holds X / 2^eX
+    // Mixed, panel in global memory: blocked Householder, Q formation and
+    // Q application, staged in the shared region (free until the Jacobi /
+    // certificate matrix A is written, and again once U is being formed).
+    const bool wy = mixed && W != sm.p + cc + c && c > kWyB && wy_stage_need(h) <= sm.cap;
+    df64* stage = reinterpret_cast<df64*>(sm.p);
+    df64* Twy = reinterpret_cast<df64*>(&sh.gemm_b[0][0]);
     if (mixed)
     {
-      const double sX = cta_pow2_of_max(X, h, c, sh);
-      cta_split_to_df(Wd, h, X, h, c, 1.0 / sX);
+      eX = pow2_exponent(cta_pow2_of_max(X, h, c, sh));
+      cta_split_to_df(Wd, h, X, h, c, -eX);
       __syncthreads();
-      cta_householder_qr_df(Wd, h, c, h, td, sh);
-      cta_extract_r_df(R, Wd, c, c, h, sX);
+      if (wy)
+        cta_householder_qr_df_wy(Wd, h, c, h, td, stage, Twy, sh);
+      else
+        cta_householder_qr_df(Wd, h, c, h, td, sh);
+      cta_extract_r_df(R, Wd, c, c, h, eX);
     }
     else
     {
@@ -160,10 +177,10 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       cta_extract_r(R, W, c, c, h);
     }
     const bool certified =
-      certify &&
-      (mixed ? cta_certify_no_truncation<df64>(R, c, h, delta, reinterpret_cast<df64*>(A), sh,
-                                               CertOps<df64>::u)
-             : cta_certify_no_truncation<double>(R, c, h, delta, A, sh, CertOps<double>::u));
+      certify && (mixed ? cta_certify_no_truncation_df(Wd, h, c, h, ldexp(delta, -eX),
+                                                       reinterpret_cast<df64*>(A), sh,
+                                                       CertOps<df64>::u)
+                        : cta_certify_no_truncation(R, c, h, delta, A, sh, CertOps<double>::u));
     int r_new = c;
     if (certified)
     {
@@ -217,13 +234,11 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
     {
       if (mixed)
       {
-        cta_form_q_df(Wd, h, c, h, td);
-        for (int64_t t = threadIdx.x; t < hc; t += blockDim.x)
-        {
-          const df64 q = Wd[t];
-          W[t] = df_to(q);
-        }
-        __syncthreads();
+        if (wy)
+          cta_form_q_df_wy(Wd, h, c, h, td, stage, Twy);
+        else
+          cta_form_q_df(Wd, h, c, h, td);
+        cta_join_from_df(W, Wd, hc);
       }
       else
         cta_form_q(W, h, c, h, tau);
@@ -235,16 +250,14 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
       for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
       {
         const int i = static_cast<int>(t % h), jj = static_cast<int>(t / h);
-        Ud[t] = i < c ? df_from(Uc[i + static_cast<int64_t>(jj) * c]) : df64{0.0f, 0.0f};
+        Ud[t] = i < c ? df_split_pow2(Uc[i + static_cast<int64_t>(jj) * c], 0) : df64{0.0f, 0.0f};
       }
       __syncthreads();
-      cta_apply_q_df(Wd, h, c, h, td, Ud, r_new, h);
-      for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * r_new; t += blockDim.x)
-      {
-        const df64 u = Ud[t];
-        U[t] = df_to(u);
-      }
-      __syncthreads();
+      if (wy)
+        cta_apply_q_df_wy(Wd, h, c, h, td, Ud, r_new, h, stage, Twy);
+      else
+        cta_apply_q_df(Wd, h, c, h, td, Ud, r_new, h);
+      cta_join_from_df(U, Ud, static_cast<int64_t>(h) * r_new);
     }
     else
     {
@@ -813,9 +826,11 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
   const bool mixed = job.mixed != 0;
   if (d <= 1)
     return;
-  int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1;
+  int64_t rmax = 1, lsum = 0, lmax = 1, hmax = 1, nmax = 1, gsum = 0;
   for (int k = 0; k < d; ++k)
   {
+    if (k >= 1)
+      gsum += static_cast<int64_t>(S[k].r) * S[k].r;
     rmax = imax64(rmax, imax64(S[k].r, S[k].rp));
     hmax = imax64(hmax, static_cast<int64_t>(S[k].r) * S[k].n);
     nmax = imax64(nmax, S[k].n);
@@ -826,28 +841,41 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
       lmax = imax64(lmax, l);
     }
   }
-  if (!fits(job, need_sketch(rmax, lsum, lmax, hmax, nmax), T))
+  if (!fits(job, need_sketch(rmax, lsum, lmax, hmax, nmax, gsum), T))
     return;
   Bump bump{scratch};
-  // 1. ||X||^2 (contract_inner_step chain, detail/contract.hpp:155-205).
-  double* E = bump.take(rmax * rmax);
-  double* En = bump.take(rmax * rmax);
+  // 1. Right Gram matrices G_k = X_{>=k} X_{>=k}^T (r_k x r_k; X_{>=k} the
+  //    r_k x (n_k ... n_{d-1}) unfolding of cores k..d-1), from k = d-1 down
+  //    (the contract_inner_step chain of detail/contract.hpp:155-205 run from
+  //    the right); G_k for k = 1..d-1 stay in gbuf for step 3, and
+  //    ||X||^2 = G_0.  gram_off(k): offset of G_k in gbuf, from the input ranks.
+  auto gram_off = [&](int k) {
+    int64_t off = 0;
+    for (int j = 1; j < k; ++j)
+      off += static_cast<int64_t>(job.pristine_slots[T.first + j].r) *
+             job.pristine_slots[T.first + j].r;
+    return off;
+  };
+  double* gbuf = bump.take(gsum);
   double* tmp = bump.take(rmax * nmax * rmax);
-  if (threadIdx.x == 0)
-    E[0] = 1.0;
-  __syncthreads();
-  for (int k = 0; k < d; ++k)
+  double* g0 = bump.take(1);
+  for (int k = d - 1; k >= 0; --k)
   {
     const int ra = S[k].r, n = S[k].n, rap = S[k].rp;
+    const int64_t w = static_cast<int64_t>(n) * rap;
     const double* ca = ar + S[k].off;
-    gemm_sel(mixed, ra, n * rap, ra, View{E, 1, ra}, View{ca, static_cast<int64_t>(n) * rap, 1},
-             tmp, static_cast<int64_t>(n) * rap, 1, sh);
-    gemm_sel(mixed, rap, rap, ra * n, View{tmp, 1, rap}, View{ca, rap, 1}, En, rap, 1, sh);
-    double* t = E;
-    E = En;
-    En = t;
+    double* Gk = k >= 1 ? gbuf + gram_off(k) : g0;
+    const double* Y = ca;  // cores k..d-1 applied to G_{k+1}: left_unfold(C_k) G_{k+1}
+    if (k < d - 1)
+    {
+      gemm_sel(mixed, ra * n, rap, rap, View{ca, rap, 1}, View{gbuf + gram_off(k + 1), rap, 1},
+               tmp, rap, 1, sh);
+      Y = tmp;
+    }
+    // G_k (ra x ra) = right_unfold(C_k) right_unfold(Y)^T.
+    gemm_sel(mixed, ra, ra, w, View{ca, w, 1}, View{Y, 1, w}, Gk, ra, 1, sh);
   }
-  const double nx2 = E[0];
+  const double nx2 = g0[0];
   __syncthreads();
   // 2. Right environments, stored for bonds 1..d-1 (wbuf + woff, woff per core).
   double* wbuf = bump.take(lsum);
@@ -884,8 +912,9 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
     Wnext = Wk;
     woff_next = woff;
   }
-  // 3. Left-to-right sketch-and-orthogonalise.
+  // 3. Left-to-right sketch-and-orthogonalise; err2 accumulates ||X - Y||^2.
   Bump step = bump;
+  double err2 = 0.0;
   for (int k = 0; k < d - 1; ++k)
   {
     Bump b2 = step;
@@ -910,6 +939,23 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
     // M (lq x rp) = Q^T left_unfold(cur).
     double* M = b2.take(static_cast<int64_t>(lq) * rp);
     gemm_sel(mixed, lq, rp, h, View{Q, h, 1}, View{ar + cur.off, rp, 1}, M, rp, 1, sh);
+    // What this projection discards: D = left_unfold(cur) - Q M (h x rp), a
+    // difference of matrices, so it is accurate to the arithmetic's unit
+    // roundoff times ||cur||.  With the cores left of k orthonormal and
+    // cores k+1.. still those of X, ||X - Y||^2 is the sum over the steps of
+    // ||D X_{>=k+1}||^2 = <D, D G_{k+1}> (the discarded parts of successive
+    // steps are mutually orthogonal).
+    double* D = b2.take(static_cast<int64_t>(h) * rp);
+    double* DG = b2.take(static_cast<int64_t>(h) * rp);
+    gemm_sel(mixed, h, rp, lq, View{Q, 1, h}, View{M, rp, 1}, D, rp, 1, sh);
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * rp; t += blockDim.x)
+      D[t] = ar[cur.off + t] - D[t];
+    __syncthreads();
+    gemm_sel(mixed, h, rp, rp, View{D, rp, 1}, View{gbuf + gram_off(k + 1), rp, 1}, DG, rp, 1, sh);
+    double part = 0.0;
+    for (int64_t t = threadIdx.x; t < static_cast<int64_t>(h) * rp; t += blockDim.x)
+      part = fma(D[t], DG[t], part);
+    err2 += cta_sum(part, sh);
     const int wn = next.n * next.rp;
     double* P = b2.take(static_cast<int64_t>(lq) * wn);
     gemm_sel(mixed, lq, wn, rp, View{M, rp, 1}, View{ar + next.off, wn, 1}, P, wn, 1, sh);
@@ -920,7 +966,6 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
     __syncthreads();
   }
   const double ny = core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh);
-  const double err2 = nx2 - ny * ny;
   const double rel = nx2 > 0.0 ? sqrt(fmax(err2, 0.0) / nx2) : 0.0;
   const bool accept = isfinite(rel) && rel <= 0.25 * job.eps;
   if (threadIdx.x == 0)

@@ -487,22 +487,22 @@ __device__ bool wide_svd_mixed(const WideJob& job, View src, int p, int q, bool 
   df64* Ad = reinterpret_cast<df64*>(job.A);
   df64* Vdd = reinterpret_cast<df64*>(job.V);
   WIDE_FOR(e, pq)
-  Ad[e] = df_from(job.A[e] * isc);
+  Ad[e] = df_split_pow2(job.A[e], -pow2_exponent(sc));
   if (with_v)
   {
     WIDE_FOR(e, qq)
-    Vdd[e] = df_from(job.V[e]);
+    Vdd[e] = df_split_pow2(job.V[e], 0);
   }
   WSYNC();
   if (!wide_jacobi<df64>(job, Ad, p, q, p, with_v ? Vdd : nullptr, job.jblock, floor2 * isc * isc,
                          kJacobiStopRel, job.max_sweeps, sm, sh, sweeps, conv))
     return false;
   WIDE_FOR(e, pq)
-  job.A[e] = df_to(Ad[e]) * sc;
+  job.A[e] = df_join_pow2(Ad[e], pow2_exponent(sc));
   if (with_v)
   {
     WIDE_FOR(e, qq)
-    job.V[e] = df_to(Vdd[e]);
+    job.V[e] = df_join_pow2(Vdd[e], 0);
   }
   WSYNC();
   return true;
