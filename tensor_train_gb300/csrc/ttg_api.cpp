@@ -6,6 +6,7 @@
 // compute path runs on the GPU; there is no host fallback.
 #include <algorithm>
 #include <atomic>
+#include <chrono>
 #include <cmath>
 #include <cstdio>
 #include <cstdlib>
@@ -609,15 +610,18 @@ int32_t layout_and_alloc(ttg_plan& P)
   const int sms = std::max(device().sms, 1);
   P.smem_doubles = P.grid > sms ? kSmemTwoPerSm : kSmemOnePerSm;
   P.cps = P.grid > sms ? 2 : 1;
-  // Large batches get scratch for up to 4 CTAs per SM (autotuner candidates)
-  // and start at 4 per SM, the autotuner's pick on the uneven 4096-TT batch
-  // (the sweeps are latency-bound: more resident TTs hide more of it).
+  // Large batches get scratch for up to 4 CTAs per SM (autotuner candidates).
+  // FP64 sweeps start at 4 per SM (DFMA-bound: more resident TTs keep the
+  // pipe fed); mixed sweeps stay at 2, whose larger shared staging holds more
+  // of the blocked df64 Householder panels -- the autotuner's picks on the
+  // uneven 4096-TT batch.
   P.scratch_ctas = P.grid;
   if (static_cast<int64_t>(P.order.size()) > 2LL * sms && P.job_kind >= 0)
   {
     P.scratch_ctas = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(P.order.size()),
                                                         4LL * sms));
-    if (static_cast<int64_t>(P.order.size()) >= 4LL * sms)
+    if (static_cast<int64_t>(P.order.size()) >= 4LL * sms &&
+        P.opts.precision != TTG_PREC_MIXED)
     {
       P.grid = P.scratch_ctas;
       P.cps = 4;
@@ -1008,10 +1012,11 @@ constexpr int kMaxDevices = 64;
 struct DeviceState
 {
   std::mutex mu;
-  std::once_flag stream_once;
+  std::once_flag stream_once, stream2_once;
   cudaStream_t stream = nullptr;
-  DevMem dev_pool;
-  HostPinned host_pool;
+  cudaStream_t stream2 = nullptr;  // the second chunk of a pipelined batch
+  DevMem dev_pool, dev_pool2;
+  HostPinned host_pool, host_pool2;
 };
 
 DeviceState g_devices[kMaxDevices];
@@ -1031,23 +1036,36 @@ cudaStream_t lib_stream()
   return s.stream;
 }
 
+cudaStream_t lib_stream2()
+{
+  DeviceState& s = dev_state();
+  std::call_once(s.stream2_once,
+                 [&] { cudaStreamCreateWithFlags(&s.stream2, cudaStreamNonBlocking); });
+  return s.stream2;
+}
+
+// Lends the device's buffers (slot 0, or slot 1 for the second plan of a
+// pipelined batch) to a plan for one call, and takes them back grown.
 struct PoolLease
 {
   ttg_plan& P;
-  DeviceState& S;
-  explicit PoolLease(ttg_plan& p) : P(p), S(dev_state())
+  DevMem& dev;
+  HostPinned& host;
+  explicit PoolLease(ttg_plan& p, int slot = 0)
+    : P(p), dev(slot ? dev_state().dev_pool2 : dev_state().dev_pool),
+      host(slot ? dev_state().host_pool2 : dev_state().host_pool)
   {
-    std::swap(P.dev.p, S.dev_pool.p);
-    std::swap(P.dev.bytes, S.dev_pool.bytes);
-    std::swap(P.host.p, S.host_pool.p);
-    std::swap(P.host.bytes, S.host_pool.bytes);
+    std::swap(P.dev.p, dev.p);
+    std::swap(P.dev.bytes, dev.bytes);
+    std::swap(P.host.p, host.p);
+    std::swap(P.host.bytes, host.bytes);
   }
   ~PoolLease()
   {
-    std::swap(P.dev.p, S.dev_pool.p);
-    std::swap(P.dev.bytes, S.dev_pool.bytes);
-    std::swap(P.host.p, S.host_pool.p);
-    std::swap(P.host.bytes, S.host_pool.bytes);
+    std::swap(P.dev.p, dev.p);
+    std::swap(P.dev.bytes, dev.bytes);
+    std::swap(P.host.p, host.p);
+    std::swap(P.host.bytes, host.bytes);
   }
 };
 
@@ -1711,6 +1729,128 @@ int32_t round_iter_impl(const ttg_tensor* in, const ttg_round_options* opts,
                          result, op);
 }
 
+// Host-side phase times of one batch call, printed to stderr when the
+// environment sets TTG_TRACE (diagnostics only: with it set, each phase
+// ends with a stream synchronize so that its time is its own).
+struct CallTrace
+{
+  bool on = std::getenv("TTG_TRACE") != nullptr;
+  std::chrono::steady_clock::time_point t = std::chrono::steady_clock::now();
+  std::string line;
+  void mark(const char* phase, cudaStream_t st = nullptr)
+  {
+    if (!on)
+      return;
+    if (st)
+      cudaStreamSynchronize(st);
+    const auto now = std::chrono::steady_clock::now();
+    char buf[64];
+    std::snprintf(buf, sizeof(buf), " %s=%.2fms", phase,
+                  std::chrono::duration<double, std::milli>(now - t).count());
+    line += buf;
+    t = now;
+  }
+  void print(const char* op, int32_t count)
+  {
+    if (on)
+      std::fprintf(stderr, "ttg_trace %s count=%d%s\n", op, count, line.c_str());
+  }
+};
+
+// Outputs and results of a finished round plan; orig maps the plan's TT t
+// to its index in the caller's arrays (null: the same).
+static int32_t unpack_round(ttg_plan& P, const int32_t* orig, ttg_tensor* outs,
+                            ttg_round_result* results, float ms)
+{
+  const char* h = static_cast<const char*>(P.host.p);
+  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
+  const int64_t n = static_cast<int64_t>(P.shapes.size());
+  return parallel_for(n, [&](int64_t ii) -> int32_t {
+    const int t = static_cast<int>(ii);
+    const int i = orig ? orig[t] : t;
+    const Shape& s = P.shapes[t];
+    if (s.d <= 1)
+    {
+      if (int32_t e = copy_through(s, &outs[i]))
+        return e;
+      if (results)
+      {
+        std::memset(&results[i], 0, sizeof(results[i]));
+        results[i].iters_run = 1;
+        results[i].converged = 1;
+      }
+      return TTG_OK;
+    }
+    if (int32_t e = emit_tensor(P, t, s.matrix, s.m, s.n, &outs[i]))
+      return e;
+    fill_result(T[t], ms, results ? &results[i] : nullptr);
+    return TTG_OK;
+  });
+}
+
+// A large batch with host buffers runs as two plans whose host and device
+// phases overlap: chunk 1 is packed and uploaded while chunk 0 sweeps, and
+// chunk 0 is downloaded and unpacked while chunk 1 sweeps.  The chunks split
+// the batch by estimated sweep cost (largest first, each TT to the lighter
+// chunk) so that the two sweeps take about as long; each sweeps on its own
+// stream, so chunk 1's CTAs take the SMs that chunk 0's last TTs free.
+constexpr int32_t kPipelineMinBatch = 1024;
+
+static int32_t round_batch_pipelined(int32_t count, const ttg_tensor* ins,
+                                     const ttg_round_options* opts, ttg_tensor* outs,
+                                     ttg_round_result* results, const char* op,
+                                     const std::vector<double>& cost)
+{
+  std::vector<int32_t> order(static_cast<size_t>(count));
+  std::iota(order.begin(), order.end(), 0);
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
+  std::vector<int32_t> part[2];
+  std::vector<ttg_tensor> cin[2];
+  double load[2] = {0.0, 0.0};
+  for (int32_t i : order)
+  {
+    const int c = load[0] <= load[1] ? 0 : 1;
+    part[c].push_back(i);
+    cin[c].push_back(ins[i]);
+    load[c] += cost[i];
+  }
+  CallTrace trace;
+  ttg_plan P0, P1;
+  ttg_plan* P[2] = {&P0, &P1};
+  PoolLease lease0(P0, 0), lease1(P1, 1);
+  const cudaStream_t st[2] = {lib_stream(), lib_stream2()};
+  for (int c = 0; c < 2; ++c)
+  {
+    if (int32_t e = build_round_plan(*P[c], static_cast<int32_t>(cin[c].size()), cin[c].data(),
+                                     opts, op))
+      return e;
+    trace.mark(c ? "pack1" : "pack0");
+    if (int32_t e = plan_upload(*P[c], st[c]))
+      return e;
+    TTG_CUDA(cudaEventRecord(P[c]->ev0, st[c]));
+    if (int32_t e = plan_run(*P[c], st[c]))
+      return e;
+    TTG_CUDA(cudaEventRecord(P[c]->ev1, st[c]));
+  }
+  for (int c = 0; c < 2; ++c)
+  {
+    if (int32_t e = plan_download_raw(*P[c], st[c]))
+      return e;
+    trace.mark(c ? "sweep1+d2h1" : "sweep0+d2h0");
+    float ms = 0.0f;
+    TTG_CUDA(cudaEventElapsedTime(&ms, P[c]->ev0, P[c]->ev1));
+    if (int32_t e = unpack_round(*P[c], part[c].data(), outs, results, ms))
+      return e;
+    trace.mark(c ? "unpack1" : "unpack0");
+  }
+  trace.print(op, count);
+  for (int c = 0; c < 2; ++c)
+    if (int32_t bad = first_bad_status(*P[c]))
+      return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
+  return TTG_OK;
+}
+
 static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_round_options* opts,
                             ttg_tensor* outs, ttg_round_result* results, const char* op)
 {
@@ -1732,44 +1872,49 @@ static int32_t round_common(int32_t count, const ttg_tensor* ins, const ttg_roun
                                     "matvec_round / matmat_round respectively.");
   // Shapes first: an invalid tensor is an argument error with or without a
   // device (the reference aborts on it before any arithmetic).
+  std::vector<double> cost(static_cast<size_t>(count), 0.0);
   for (int32_t i = 0; i < count; ++i)
   {
     Shape s;
     if (int32_t st = describe(&ins[i], op, s))
       return st;
+    for (int k = 0; k < s.d; ++k)  // ~ flops of the step at core k
+      cost[i] += static_cast<double>(s.r[k]) * s.mode(k) * s.r[k + 1] * std::max(s.r[k], s.r[k + 1]);
   }
   if (int32_t st = need_device())
     return st;
   std::lock_guard<std::mutex> lk(dev_state().mu);
+  if (count >= kPipelineMinBatch && opts->method == TTG_METHOD_SVD && !opts->bond_stats &&
+      (opts->schedule == TTG_SCHED_AUTO || opts->schedule == TTG_SCHED_PER_TT))
+    return round_batch_pipelined(count, ins, opts, outs, results, op, cost);
+  CallTrace trace;
   ttg_plan P;
   PoolLease lease(P);
   if (int32_t st = build_round_plan(P, count, ins, opts, op))
     return st;
+  trace.mark("plan+pack");
   float ms = 0.0f;
-  if (int32_t st = execute(P, &ms))
-    return st;
-  const char* h = static_cast<const char*>(P.host.p);
-  const TTInfo* T = reinterpret_cast<const TTInfo*>(h + P.off_tts);
-  const int32_t est = parallel_for(count, [&](int64_t ii) -> int32_t {
-    const int i = static_cast<int>(ii);
-    const Shape& s = P.shapes[i];
-    if (s.d <= 1)
-    {
-      if (int32_t e = copy_through(s, &outs[i]))
-        return e;
-      if (results)
-      {
-        std::memset(&results[i], 0, sizeof(results[i]));
-        results[i].iters_run = 1;
-        results[i].converged = 1;
-      }
-      return TTG_OK;
-    }
-    if (int32_t e = emit_tensor(P, i, s.matrix, s.m, s.n, &outs[i]))
+  if (trace.on)
+  {
+    cudaStream_t st = lib_stream();
+    if (int32_t e = plan_upload(P, st))
       return e;
-    fill_result(T[i], ms, results ? &results[i] : nullptr);
-    return TTG_OK;
-  });
+    trace.mark("h2d", st);
+    TTG_CUDA(cudaEventRecord(P.ev0, st));
+    if (int32_t e = plan_run(P, st))
+      return e;
+    TTG_CUDA(cudaEventRecord(P.ev1, st));
+    trace.mark("run", st);
+    if (int32_t e = plan_download_raw(P, st))
+      return e;
+    trace.mark("d2h", st);
+    TTG_CUDA(cudaEventElapsedTime(&ms, P.ev0, P.ev1));
+  }
+  else if (int32_t st = execute(P, &ms))
+    return st;
+  const int32_t est = unpack_round(P, nullptr, outs, results, ms);
+  trace.mark("unpack");
+  trace.print(op, count);
   if (est)
     return est;
   if (int32_t bad = first_bad_status(P))
