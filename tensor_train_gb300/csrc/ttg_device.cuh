@@ -349,63 +349,104 @@ __device__ int trunc_rank_serial(const double* s, int n, double delta, int max_r
 // memory, 4x4 register tile per thread.
 // ---------------------------------------------------------------------------
 // One 64x64 output tile at (i0, j0).
+// Zero structure a GEMM may skip: A(i, p) = 0 for p < i (an upper-
+// triangular left factor, R of a QR), or B(p, j) = 0 for p < j (a lower-
+// triangular right factor, R^T).
+enum GemmTri : int
+{
+  kTriNone = 0,
+  kTriUpperA = 1,
+  kTriLowerB = 2,
+};
+
+// Rows (or columns) ty + 16 a, a < result, of a thread's 4 x 4 block that
+// lie inside the matrix (extent m from the tile start) and, for a
+// triangular factor, can be non-zero in the k slab [p0, p0 + 16) (index
+// <= p0 + 15 - tile start).
+__device__ __forceinline__ int gemm_live(int m_from_tile, int t, bool tri, int p0_from_tile)
+{
+  int n = (m_from_tile - t + 15) >> 4;
+  if (tri)
+  {
+    const int q = p0_from_tile + 15 - t;
+    const int nt = q < 0 ? 0 : (q >> 4) + 1;
+    n = nt < n ? nt : n;
+  }
+  return n < 0 ? 0 : (n > 4 ? 4 : n);
+}
+
+// One 64 x 64 tile of C = A B (FP64): k slabs of 16 staged in shared
+// memory, 4 x 4 outputs per thread.  A thread multiplies only the rows and
+// columns of its block that are inside the matrix and, under tri, not in
+// the zero triangle of the slab; slabs left of the diagonal are skipped.
 __device__ void cta_gemm_tile(int i0, int j0, int M, int N, int K, View A, View B, double* C,
-                              int64_t c_rs, int64_t c_cs, CtaShared& sh)
+                              int64_t c_rs, int64_t c_cs, CtaShared& sh, int tri)
 {
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
+  double acc[4][4];
+#pragma unroll
+  for (int a = 0; a < 4; ++a)
+#pragma unroll
+    for (int b = 0; b < 4; ++b)
+      acc[a][b] = 0.0;
+  const int pstart = tri == kTriUpperA ? i0 : (tri == kTriLowerB ? j0 : 0);
+  for (int p0 = pstart; p0 < K; p0 += 16)
+  {
+    __syncthreads();
+    for (int t = threadIdx.x; t < 16 * 64; t += blockDim.x)
     {
-      double acc[4][4];
+      const int kk = t / 64, ii = t % 64;
+      const int gi = i0 + ii, gp = p0 + kk, gj = j0 + ii;
+      sh.gemm_a[kk][ii] = (gi < M && gp < K) ? A(gi, gp) : 0.0;
+      sh.gemm_b[kk][ii] = (gp < K && gj < N) ? B(gp, gj) : 0.0;
+    }
+    __syncthreads();
+    const int na = gemm_live(M - i0, ty, tri == kTriUpperA, p0 - i0);
+    const int nb = gemm_live(N - j0, tx, tri == kTriLowerB, p0 - j0);
+    const int kmax = K - p0 < 16 ? K - p0 : 16;
+#pragma unroll 4
+    for (int kk = 0; kk < kmax; ++kk)
+    {
+      double av[4], bv[4];
 #pragma unroll
       for (int a = 0; a < 4; ++a)
+        av[a] = sh.gemm_a[kk][ty + 16 * a];
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-          acc[a][b] = 0.0;
-      for (int p0 = 0; p0 < K; p0 += 16)
-      {
-        __syncthreads();
-        for (int t = threadIdx.x; t < 16 * 64; t += blockDim.x)
+      for (int b = 0; b < 4; ++b)
+        bv[b] = sh.gemm_b[kk][tx + 16 * b];
+#pragma unroll
+      for (int a = 0; a < 4; ++a)
+        if (a < na)
         {
-          const int kk = t / 64, ii = t % 64;
-          const int gi = i0 + ii, gp = p0 + kk, gj = j0 + ii;
-          sh.gemm_a[kk][ii] = (gi < M && gp < K) ? A(gi, gp) : 0.0;
-          sh.gemm_b[kk][ii] = (gp < K && gj < N) ? B(gp, gj) : 0.0;
-        }
-        __syncthreads();
-#pragma unroll
-        for (int kk = 0; kk < 16; ++kk)
-        {
-          double av[4], bv[4];
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-            av[a] = sh.gemm_a[kk][ty + 16 * a];
 #pragma unroll
           for (int b = 0; b < 4; ++b)
-            bv[b] = sh.gemm_b[kk][tx + 16 * b];
-#pragma unroll
-          for (int a = 0; a < 4; ++a)
-#pragma unroll
-            for (int b = 0; b < 4; ++b)
+            if (b < nb)
               acc[a][b] = fma(av[a], bv[b], acc[a][b]);
         }
-      }
+    }
+  }
 #pragma unroll
-      for (int a = 0; a < 4; ++a)
+  for (int a = 0; a < 4; ++a)
 #pragma unroll
-        for (int b = 0; b < 4; ++b)
-        {
-          const int gi = i0 + ty + 16 * a, gj = j0 + tx + 16 * b;
-          if (gi < M && gj < N)
-            C[gi * c_rs + gj * c_cs] = acc[a][b];
-        }
+    for (int b = 0; b < 4; ++b)
+    {
+      const int gi = i0 + ty + 16 * a, gj = j0 + tx + 16 * b;
+      if (gi < M && gj < N)
+        C[gi * c_rs + gj * c_cs] = acc[a][b];
     }
 }
 
+// C = A B, tile by tile (row tiles outer).  With tri = kTriUpperA a tile
+// reads B only from its own first row down, and with kTriLowerB A only from
+// its own first column right; so C may be B itself (upper A, M <= K, same
+// layout) or A itself (lower B, N <= K, same layout): every element is read
+// by the tiles that need it before a tile writes over it.
 __device__ __noinline__ void cta_gemm(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
-                         int64_t c_cs, CtaShared& sh)
+                         int64_t c_cs, CtaShared& sh, int tri = kTriNone)
 {
   for (int i0 = 0; i0 < M; i0 += 64)
     for (int j0 = 0; j0 < N; j0 += 64)
-      cta_gemm_tile(i0, j0, M, N, K, A, B, C, c_rs, c_cs, sh);
+      cta_gemm_tile(i0, j0, M, N, K, A, B, C, c_rs, c_cs, sh, tri);
   __syncthreads();
 }
 

@@ -855,10 +855,11 @@ __device__ __noinline__ int cta_jacobi_mixed(View src, int m, int n, double* A, 
 
 // C(i, j) = sum_p A(i, p) B(p, j) in df64 (FP64 in, FP64 out).  A and B are
 // scaled by powers of two (exact) so the split never leaves FP32 range.
+// tri and in-place use as cta_gemm (the same tiles, rows and slabs).
 // 64x64 output tiles, 16-deep k slabs in shared memory (the df64 slabs reuse
 // the CtaShared GEMM buffers, one df64 per double slot), 4x4 per thread.
 __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, double* C, int64_t c_rs,
-                            int64_t c_cs, CtaShared& sh)
+                            int64_t c_cs, CtaShared& sh, int tri = kTriNone)
 {
   const int ea = pow2_exponent(cta_pow2_of_max(A, M, K, sh));
   const int eb = pow2_exponent(cta_pow2_of_max(B, K, N, sh));
@@ -874,7 +875,8 @@ __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, do
 #pragma unroll
         for (int b = 0; b < 4; ++b)
           acc[a][b] = df64{0.0f, 0.0f};
-      for (int p0 = 0; p0 < K; p0 += 16)
+      const int pstart = tri == kTriUpperA ? i0 : (tri == kTriLowerB ? j0 : 0);
+      for (int p0 = pstart; p0 < K; p0 += 16)
       {
         __syncthreads();
         for (int t = threadIdx.x; t < 16 * 64; t += blockDim.x)
@@ -885,8 +887,11 @@ __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, do
           bs[kk][ii] = (gp < K && gj < N) ? df_split_pow2(B(gp, gj), -eb) : df64{0.0f, 0.0f};
         }
         __syncthreads();
+        const int na = gemm_live(M - i0, ty, tri == kTriUpperA, p0 - i0);
+        const int nb = gemm_live(N - j0, tx, tri == kTriLowerB, p0 - j0);
+        const int kmax = K - p0 < 16 ? K - p0 : 16;
 #pragma unroll 4
-        for (int kk = 0; kk < 16; ++kk)
+        for (int kk = 0; kk < kmax; ++kk)
         {
           df64 av[4], bv[4];
 #pragma unroll
@@ -897,9 +902,13 @@ __device__ __noinline__ void cta_gemm_df(int M, int N, int K, View A, View B, do
             bv[b] = bs[kk][tx + 16 * b];
 #pragma unroll
           for (int a = 0; a < 4; ++a)
+            if (a < na)
+            {
 #pragma unroll
-            for (int b = 0; b < 4; ++b)
-              acc[a][b] = df_fma(av[a], bv[b], acc[a][b]);
+              for (int b = 0; b < 4; ++b)
+                if (b < nb)
+                  acc[a][b] = df_fma(av[a], bv[b], acc[a][b]);
+            }
         }
       }
 #pragma unroll

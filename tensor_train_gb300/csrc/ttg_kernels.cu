@@ -42,12 +42,12 @@ struct GemmDf
 };
 
 __device__ void gemm_sel(bool mixed, int M, int N, int K, View A, View B, double* C, int64_t rs,
-                         int64_t cs, CtaShared& sh)
+                         int64_t cs, CtaShared& sh, int tri = kTriNone)
 {
   if (mixed)
-    cta_gemm_df(M, N, K, A, B, C, rs, cs, sh);
+    cta_gemm_df(M, N, K, A, B, C, rs, cs, sh, tri);
   else
-    cta_gemm(M, N, K, A, B, C, rs, cs, sh);
+    cta_gemm(M, N, K, A, B, C, rs, cs, sh, tri);
 }
 
 // Dynamic shared memory of the CTA, used to stage the matrix a step works
@@ -56,8 +56,10 @@ __device__ void gemm_sel(bool mixed, int M, int N, int K, View A, View B, double
 // QR of X (h x c).  Q -> *W (h x k, column-major, ld h), R -> R (k x c,
 // column-major, ld k), k = min(h, c).  The factorisation runs in shared
 // memory when h*c fits there, else in Wg; *W tells the caller where Q is.
+// qdst (mixed only, optional): Q is rounded to FP64 straight into qdst
+// (h*k doubles; it may be X's storage, which is read before), and *W = qdst.
 __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* tau, double* R, Smem sm,
-                         double** Wout, bool mixed, CtaShared& sh)
+                         double** Wout, bool mixed, CtaShared& sh, double* qdst = nullptr)
 {
   double* W = (static_cast<int64_t>(h) * c <= sm.cap) ? sm.p : Wg;
   *Wout = W;
@@ -84,7 +86,9 @@ __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* 
       cta_form_q_df_wy(Wd, h, k, h, td, stage, T);
     else
       cta_form_q_df(Wd, h, k, h, td);
-    cta_join_from_df(W, Wd, static_cast<int64_t>(h) * k);
+    if (qdst)
+      *Wout = qdst;
+    cta_join_from_df(qdst ? qdst : W, Wd, static_cast<int64_t>(h) * k);
     return k;
   }
   cta_copy_to_colmajor(W, h, X, h, c);
@@ -105,11 +109,15 @@ __device__ __noinline__ int qr_factor(View X, int h, int c, double* Wg, double* 
 // transpose, accumulating V) when h < c.
 
 // s_out (optional) receives the singular values, descending (c or h of them).
+// f_upper (optional) is set when F is the upper-triangular R of the QR
+// (a certified bond): the caller's absorption may skip its zero triangle.
 __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max_rank, int max_sweeps,
                         bool mixed, Bump bump, Smem sm, double** Ut_out, double** F_out,
                         TTInfo& T, CtaShared& sh, BondStat* bs = nullptr,
-                        double** s_out = nullptr)
+                        double** s_out = nullptr, bool* f_upper = nullptr)
 {
+  if (f_upper)
+    *f_upper = false;
   double* sig;
   double* sorted;
   int* ord;
@@ -271,6 +279,8 @@ __device__ __noinline__ int left_svd(View X, int h, int c, double delta, int max
     }
     if (!certified)
       record_bond(bs, sorted, c, r_new);
+    if (certified && f_upper)
+      *f_upper = true;
     if (threadIdx.x == 0)
     {
       if (!certified && !finite(sorted[0]))
@@ -443,11 +453,20 @@ __device__ __noinline__ void right_qr_step(double* ar, CoreSlot& cur, CoreSlot& 
   double* R = bump.take(static_cast<int64_t>(r) * r);
   double* P = bump.take(static_cast<int64_t>(hp) * r);
   double* Q;
-  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sm, &Q, mixed, sh);
-  // prev (hp x k) = left_unfold(prev) (hp x r) * L, L(a, e) = R(e, a).
-  gemm_sel(mixed, hp, k, r, View{ps, r, 1}, View{R, k, 1}, P, k, 1, sh);
-  cta_copy(ps, P, static_cast<int64_t>(hp) * k);
-  cta_copy(cs, Q, static_cast<int64_t>(w) * k);
+  // Q (w x k column-major) is the new right_unfold(cur) (k x w row-major):
+  // the mixed path writes it there directly.
+  const int k = qr_factor(View{cs, 1, w}, w, r, W, tau, R, sm, &Q, mixed, sh, mixed ? cs : nullptr);
+  // prev (hp x k) = left_unfold(prev) (hp x r) * L, L(a, e) = R(e, a)
+  // (lower triangular); in place when the rank stays r.
+  if (k == r)
+    gemm_sel(mixed, hp, k, r, View{ps, r, 1}, View{R, k, 1}, ps, k, 1, sh, kTriLowerB);
+  else
+  {
+    gemm_sel(mixed, hp, k, r, View{ps, r, 1}, View{R, k, 1}, P, k, 1, sh, kTriLowerB);
+    cta_copy(ps, P, static_cast<int64_t>(hp) * k);
+  }
+  if (Q != cs)
+    cta_copy(cs, Q, static_cast<int64_t>(w) * k);
   set_ranks(cur, k, rp);
   set_ranks(prev, prev.r, k);
   __syncthreads();
@@ -468,9 +487,15 @@ __device__ __noinline__ void left_qr_step(double* ar, CoreSlot& cur, CoreSlot& n
   double* P = bump.take(static_cast<int64_t>(rp) * wn);
   double* Q;
   const int k = qr_factor(View{cs, rp, 1}, h, rp, W, tau, R, sm, &Q, mixed, sh);
-  // next (k x wn) = R (k x rp) * right_unfold(next) (rp x wn).
-  gemm_sel(mixed, k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, P, wn, 1, sh);
-  cta_copy(ns, P, static_cast<int64_t>(k) * wn);
+  // next (k x wn) = R (k x rp, upper triangular) * right_unfold(next)
+  // (rp x wn); in place when the rank stays rp.
+  if (k == rp)
+    gemm_sel(mixed, k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, ns, wn, 1, sh, kTriUpperA);
+  else
+  {
+    gemm_sel(mixed, k, wn, rp, View{R, 1, k}, View{ns, wn, 1}, P, wn, 1, sh, kTriUpperA);
+    cta_copy(ns, P, static_cast<int64_t>(k) * wn);
+  }
   // cur row-major (h x k) <- Q column-major.
   cta_copy_to_rowmajor(cs, k, View{Q, 1, h}, h, k);
   set_ranks(cur, r, k);
@@ -490,10 +515,18 @@ __device__ __noinline__ void svd_step(const RoundJob& job, double* ar, CoreSlot&
   double* ns = ar + next.off;
   double* P = bump.take(static_cast<int64_t>(c) * wn);
   double *U, *F;
+  bool f_upper = false;
   const int r_new = left_svd(View{cs, c, 1}, h, c, delta, job.max_rank, job.max_sweeps,
-                             job.mixed != 0, bump, sm, &U, &F, T, sh, bs);
-  gemm_sel(job.mixed != 0, r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, P, wn, 1, sh);
-  cta_copy(ns, P, static_cast<int64_t>(r_new) * wn);
+                             job.mixed != 0, bump, sm, &U, &F, T, sh, bs, nullptr, &f_upper);
+  // A certified bond keeps F = R (c x c, upper triangular): in place.
+  if (f_upper)
+    gemm_sel(job.mixed != 0, r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, ns, wn, 1, sh,
+             kTriUpperA);
+  else
+  {
+    gemm_sel(job.mixed != 0, r_new, wn, c, View{F, c, 1}, View{ns, wn, 1}, P, wn, 1, sh);
+    cta_copy(ns, P, static_cast<int64_t>(r_new) * wn);
+  }
   cta_copy_to_rowmajor(cs, r_new, View{U, 1, h}, h, r_new);
   set_ranks(cur, r, r_new);
   set_ranks(next, r_new, next.rp);
@@ -511,11 +544,19 @@ __device__ __noinline__ void svd_step_right(const RoundJob& job, double* ar, Cor
   double* ps = ar + prev.off;
   double* P = bump.take(static_cast<int64_t>(hp) * r);
   double *U, *F;
+  bool f_upper = false;
   const int r_new = left_svd(View{cs, 1, w}, w, r, delta, job.max_rank, job.max_sweeps,
-                             job.mixed != 0, bump, sm, &U, &F, T, sh);
-  // prev (hp x r_new) = left_unfold(prev) (hp x r) * F^T.
-  gemm_sel(job.mixed != 0, hp, r_new, r, View{ps, r, 1}, View{F, 1, r}, P, r_new, 1, sh);
-  cta_copy(ps, P, static_cast<int64_t>(hp) * r_new);
+                             job.mixed != 0, bump, sm, &U, &F, T, sh, nullptr, nullptr, &f_upper);
+  // prev (hp x r_new) = left_unfold(prev) (hp x r) * F^T; a certified bond
+  // keeps F = R (r x r), so F^T is lower triangular: in place.
+  if (f_upper)
+    gemm_sel(job.mixed != 0, hp, r_new, r, View{ps, r, 1}, View{F, 1, r}, ps, r_new, 1, sh,
+             kTriLowerB);
+  else
+  {
+    gemm_sel(job.mixed != 0, hp, r_new, r, View{ps, r, 1}, View{F, 1, r}, P, r_new, 1, sh);
+    cta_copy(ps, P, static_cast<int64_t>(hp) * r_new);
+  }
   cta_copy(cs, U, static_cast<int64_t>(w) * r_new);
   set_ranks(cur, r_new, rp);
   set_ranks(prev, prev.r, r_new);

@@ -139,7 +139,7 @@ __device__ bool wide_gemm(const WideJob& job, int M, int N, int K, View A, View 
   }
   const int tm = (M + 63) / 64, tn = (N + 63) / 64;
   for (int t = job.rank; t < tm * tn; t += job.size)
-    cta_gemm_tile((t / tn) * 64, (t % tn) * 64, M, N, K, A, B, C, c_rs, c_cs, sh);
+    cta_gemm_tile((t / tn) * 64, (t % tn) * 64, M, N, K, A, B, C, c_rs, c_cs, sh, kTriNone);
   __syncthreads();
   return true;
 }
