@@ -118,6 +118,25 @@ __device__ void cta_copy_to_rowmajor(double* dst, int64_t ld, View src, int64_t 
   }
 }
 
+// Lanes per column in the column loops of the unblocked Householder
+// routines, by the column's length: short columns put several columns in
+// flight per warp (each with a shorter reduction: in FP64 every level is an
+// add on the FP64 pipe, for all 32 lanes) instead of chaining five levels
+// per column.  Uniform over the CTA.
+__device__ __forceinline__ int hh_group(int len)
+{
+  return len > 192 ? 32 : (len > 64 ? 16 : 8);
+}
+
+// Sum over the G aligned lanes of a group (G = 8, 16 or 32); every lane of
+// the group gets it.  All 32 lanes of the warp must call it.
+__device__ __forceinline__ double group_sum(double v, int G)
+{
+  for (int o = G >> 1; o > 0; o >>= 1)
+    v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
 // ---------------------------------------------------------------------------
 // Householder QR, in place.  A column-major (m x c, ld).  On return the
 // upper triangle of the leading (k x c) block holds R (k = min(m, c)), the
@@ -183,20 +202,30 @@ __device__ __noinline__ void cta_householder_qr(double* A, int m, int c, int64_t
     const double t = sh.hh[0], inv = sh.hh[1];
     if (t != 0.0)
     {
-      for (int col = j + 1 + w; col < c; col += kWarps)
+      // G lanes per column, 32 / G columns in flight per warp; the loop
+      // bound is uniform over the warp (the group sum needs every lane).
+      const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+      for (int cb = j + 1 + w * gpw; cb < c; cb += kWarps * gpw)
       {
-        double* y = A + col * ld + j;
+        const int col = cb + lane / G;
+        const bool act = col < c;
+        double* y = A + (act ? col : cb) * ld + j;
         double dot = 0.0;
-        for (int i = 1 + lane; i < len; i += 32)
-          dot = fma(x[i], y[i], dot);
-        // t (y0 + v1..^T y1..), v = x * inv: lane 0 alone reads and writes y0.
-        const double y0 = (lane == 0) ? y[0] : 0.0;
-        dot = warp_sum(fma(dot, inv, y0)) * t;
-        const double nd = -dot * inv;
-        if (lane == 0)
-          y[0] = y0 - dot;
-        for (int i = 1 + lane; i < len; i += 32)
-          y[i] = fma(nd, x[i], y[i]);
+        if (act)
+          for (int i = 1 + gl; i < len; i += G)
+            dot = fma(x[i], y[i], dot);
+        // t (y0 + v1..^T y1..), v = x * inv: the group's lane 0 alone reads
+        // and writes y0.
+        const double y0 = (act && gl == 0) ? y[0] : 0.0;
+        dot = group_sum(fma(dot, inv, y0), G) * t;
+        if (act)
+        {
+          const double nd = -dot * inv;
+          if (gl == 0)
+            y[0] = y0 - dot;
+          for (int i = 1 + gl; i < len; i += G)
+            y[i] = fma(nd, x[i], y[i]);
+        }
       }
     }
     inv_prev = inv;
@@ -236,15 +265,20 @@ __device__ __noinline__ void cta_form_q(double* A, int m, int k, int64_t ld, con
     const int len = m - j;
     if (t != 0.0)
     {
-      for (int col = j + 1 + w; col < k; col += kWarps)
+      const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+      for (int cb = j + 1 + w * gpw; cb < k; cb += kWarps * gpw)
       {
-        double* y = A + col * ld + j;
+        const int col = cb + lane / G;
+        const bool act = col < k;
+        double* y = A + (act ? col : cb) * ld + j;
         double dot = 0.0;
-        for (int i = lane; i < len; i += 32)
-          dot += (i == 0 ? 1.0 : v[i]) * y[i];
-        dot = warp_sum(dot) * t;
-        for (int i = lane; i < len; i += 32)
-          y[i] -= dot * (i == 0 ? 1.0 : v[i]);
+        if (act)
+          for (int i = gl; i < len; i += G)
+            dot = fma(i == 0 ? 1.0 : v[i], y[i], dot);
+        dot = group_sum(dot, G) * t;
+        if (act)
+          for (int i = gl; i < len; i += G)
+            y[i] = fma(-dot, i == 0 ? 1.0 : v[i], y[i]);
       }
     }
     __syncthreads();
@@ -270,15 +304,20 @@ __device__ __noinline__ void cta_apply_q(const double* A, int m, int kref, int64
       continue;
     const double* v = A + j * lda + j;
     const int len = m - j;
-    for (int col = w; col < p; col += kWarps)
+    const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+    for (int cb = w * gpw; cb < p; cb += kWarps * gpw)
     {
-      double* y = B + col * ldb + j;
+      const int col = cb + lane / G;
+      const bool act = col < p;
+      double* y = B + (act ? col : cb) * ldb + j;
       double dot = 0.0;
-      for (int i = lane; i < len; i += 32)
-        dot += (i == 0 ? 1.0 : v[i]) * y[i];
-      dot = warp_sum(dot) * t;
-      for (int i = lane; i < len; i += 32)
-        y[i] -= dot * (i == 0 ? 1.0 : v[i]);
+      if (act)
+        for (int i = gl; i < len; i += G)
+          dot = fma(i == 0 ? 1.0 : v[i], y[i], dot);
+      dot = group_sum(dot, G) * t;
+      if (act)
+        for (int i = gl; i < len; i += G)
+          y[i] = fma(-dot, i == 0 ? 1.0 : v[i], y[i]);
     }
     __syncthreads();
   }

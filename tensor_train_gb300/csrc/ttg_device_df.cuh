@@ -92,6 +92,15 @@ __device__ void cta_join_from_df(double* W, const df64* A, int64_t n)
   __syncthreads();
 }
 
+// Sum over the G aligned lanes of a group (G = 8, 16 or 32); every lane of
+// the group gets it.  All 32 lanes of the warp must call it.
+__device__ __forceinline__ df64 df_group_sum(df64 v, int G)
+{
+  for (int o = G >> 1; o > 0; o >>= 1)
+    v = df_add(v, df_shfl_xor(v, o));
+  return v;
+}
+
 // The reflector of x = (x0, x1..) with ||x1..||^2 = tail2, in df64 on the
 // FP32 pipes: H = I - t v v^T, v = (1, x1.. * inv), H x = (beta, 0..);
 // t = 0 (no reflection) when the tail is negligible.
@@ -157,20 +166,30 @@ __device__ __noinline__ void cta_householder_qr_df(df64* A, int m, int c, int64_
     }
     if (td.hi != 0.0f)
     {
-      for (int col = j + 1 + w; col < c; col += kWarps)
+      // G lanes per column, 32 / G columns in flight per warp; the loop
+      // bound is uniform over the warp (the group sum needs every lane).
+      const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+      for (int cb = j + 1 + w * gpw; cb < c; cb += kWarps * gpw)
       {
-        df64* y = A + col * ld + j;
+        const int col = cb + lane / G;
+        const bool act = col < c;
+        df64* y = A + (act ? col : cb) * ld + j;
         df64 dot{0.0f, 0.0f};
-        for (int i = 1 + lane; i < len; i += 32)
-          dot = df_fma(x[i], y[i], dot);
-        // t (y0 + v1..^T y1..), v = x * inv: lane 0 alone reads and writes y0.
-        const df64 y0 = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
-        dot = df_mul(df_warp_sum(df_fma(dot, inv, y0)), td);
-        const df64 nd = df_neg(df_mul(dot, inv));
-        if (lane == 0)
-          y[0] = df_sub(y0, dot);
-        for (int i = 1 + lane; i < len; i += 32)
-          y[i] = df_fma(nd, x[i], y[i]);
+        if (act)
+          for (int i = 1 + gl; i < len; i += G)
+            dot = df_fma(x[i], y[i], dot);
+        // t (y0 + v1..^T y1..), v = x * inv: the group's lane 0 alone reads
+        // and writes y0.
+        const df64 y0 = (act && gl == 0) ? y[0] : df64{0.0f, 0.0f};
+        dot = df_mul(df_group_sum(df_fma(dot, inv, y0), G), td);
+        if (act)
+        {
+          const df64 nd = df_neg(df_mul(dot, inv));
+          if (gl == 0)
+            y[0] = df_sub(y0, dot);
+          for (int i = 1 + gl; i < len; i += G)
+            y[i] = df_fma(nd, x[i], y[i]);
+        }
       }
     }
     inv_prev = inv;
@@ -208,18 +227,25 @@ __device__ __noinline__ void cta_form_q_df(df64* A, int m, int k, int64_t ld, co
     const int len = m - j;
     if (t.hi != 0.0f)
     {
-      for (int col = j + 1 + w; col < k; col += kWarps)
+      const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+      for (int cb = j + 1 + w * gpw; cb < k; cb += kWarps * gpw)
       {
-        df64* y = A + col * ld + j;
-        df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
-        for (int i = 1 + lane; i < len; i += 32)
-          dot = df_fma(v[i], y[i], dot);
-        dot = df_mul(df_warp_sum(dot), t);
-        const df64 nd = df_neg(dot);
-        if (lane == 0)
-          y[0] = df_add(y[0], nd);
-        for (int i = 1 + lane; i < len; i += 32)
-          y[i] = df_fma(nd, v[i], y[i]);
+        const int col = cb + lane / G;
+        const bool act = col < k;
+        df64* y = A + (act ? col : cb) * ld + j;
+        df64 dot = (act && gl == 0) ? y[0] : df64{0.0f, 0.0f};
+        if (act)
+          for (int i = 1 + gl; i < len; i += G)
+            dot = df_fma(v[i], y[i], dot);
+        dot = df_mul(df_group_sum(dot, G), t);
+        if (act)
+        {
+          const df64 nd = df_neg(dot);
+          if (gl == 0)
+            y[0] = df_add(y[0], nd);
+          for (int i = 1 + gl; i < len; i += G)
+            y[i] = df_fma(nd, v[i], y[i]);
+        }
       }
     }
     __syncthreads();
@@ -246,18 +272,25 @@ __device__ __noinline__ void cta_apply_q_df(const df64* A, int m, int kref, int6
       continue;
     const df64* v = A + j * lda + j;
     const int len = m - j;
-    for (int col = w; col < p; col += kWarps)
+    const int G = hh_group(len), gpw = 32 / G, gl = lane & (G - 1);
+    for (int cb = w * gpw; cb < p; cb += kWarps * gpw)
     {
-      df64* y = B + col * ldb + j;
-      df64 dot = (lane == 0) ? y[0] : df64{0.0f, 0.0f};
-      for (int i = 1 + lane; i < len; i += 32)
-        dot = df_fma(v[i], y[i], dot);
-      dot = df_mul(df_warp_sum(dot), t);
-      const df64 nd = df_neg(dot);
-      if (lane == 0)
-        y[0] = df_add(y[0], nd);
-      for (int i = 1 + lane; i < len; i += 32)
-        y[i] = df_fma(nd, v[i], y[i]);
+      const int col = cb + lane / G;
+      const bool act = col < p;
+      df64* y = B + (act ? col : cb) * ldb + j;
+      df64 dot = (act && gl == 0) ? y[0] : df64{0.0f, 0.0f};
+      if (act)
+        for (int i = 1 + gl; i < len; i += G)
+          dot = df_fma(v[i], y[i], dot);
+      dot = df_mul(df_group_sum(dot, G), t);
+      if (act)
+      {
+        const df64 nd = df_neg(dot);
+        if (gl == 0)
+          y[0] = df_add(y[0], nd);
+        for (int i = 1 + gl; i < len; i += G)
+          y[i] = df_fma(nd, v[i], y[i]);
+      }
     }
     __syncthreads();
   }
