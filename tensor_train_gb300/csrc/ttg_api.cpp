@@ -612,20 +612,21 @@ int32_t layout_and_alloc(ttg_plan& P)
   P.cps = P.grid > sms ? 2 : 1;
   // Large batches get scratch for up to 4 CTAs per SM (autotuner candidates).
   // FP64 sweeps start at 4 per SM (DFMA-bound: more resident TTs keep the
-  // pipe fed); mixed sweeps stay at 2, whose larger shared staging holds more
-  // of the blocked df64 Householder panels -- the autotuner's picks on the
+  // pipe fed); mixed sweeps at 3, whose 56 KB of shared staging still holds
+  // the blocked df64 Householder panels -- the autotuner's picks on the
   // uneven 4096-TT batch.
   P.scratch_ctas = P.grid;
   if (static_cast<int64_t>(P.order.size()) > 2LL * sms && P.job_kind >= 0)
   {
     P.scratch_ctas = static_cast<int>(std::min<int64_t>(static_cast<int64_t>(P.order.size()),
                                                         4LL * sms));
-    if (static_cast<int64_t>(P.order.size()) >= 4LL * sms &&
-        P.opts.precision != TTG_PREC_MIXED)
+    const bool mixed = P.opts.precision == TTG_PREC_MIXED;
+    const int cps = mixed ? 3 : 4;
+    if (static_cast<int64_t>(P.order.size()) >= static_cast<int64_t>(cps) * sms)
     {
-      P.grid = P.scratch_ctas;
-      P.cps = 4;
-      P.smem_doubles = kSmemFourPerSm;
+      P.grid = cps * sms;
+      P.cps = cps;
+      P.smem_doubles = mixed ? kSmemThreePerSm : kSmemFourPerSm;
     }
   }
   size_t o = 0;

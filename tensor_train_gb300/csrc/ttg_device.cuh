@@ -125,7 +125,7 @@ __device__ void cta_copy_to_rowmajor(double* dst, int64_t ld, View src, int64_t 
 // per column.  Uniform over the CTA.
 __device__ __forceinline__ int hh_group(int len)
 {
-  return len > 192 ? 32 : (len > 64 ? 16 : 8);
+  return len > 256 ? 32 : (len > 96 ? 16 : 8);
 }
 
 // Sum over the G aligned lanes of a group (G = 8, 16 or 32); every lane of

@@ -85,46 +85,55 @@ __device__ void wy_build_t_df(const df64* P, int hp, int nb, const df64* tau, df
 // B(0:hp, 0:ncols) <- (I - V T' V^T) B, T' = T^T (kTrans: the product
 // H_{j0+nb-1} ... H_j0, as the factorisation applies the block) or T (the
 // product H_j0 ... H_{j0+nb-1}).  B points at the block's first row,
-// column stride ldb.  One warp per column of B.  Ends with a barrier.
+// column stride ldb.  A group of hh_group(hp) lanes per column of B.  Ends
+// with a barrier.
 template <bool kTrans>
 __device__ __noinline__ void wy_apply_df(const df64* P, int hp, const df64* T, df64* B, int64_t ldb,
                                          int ncols)
 {
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int li = lane & (kWyB - 1);
-  for (int q = w; q < ncols; q += kWarps)
+  // G lanes per column (hh_group), 32 / G columns in flight per warp; the
+  // loop bound is uniform over the warp (the group sums need every lane).
+  const int G = hh_group(hp), gpw = 32 / G, gl = lane & (G - 1), gbase = lane & ~(G - 1);
+  const int li = gl & (kWyB - 1);
+  for (int cb = w * gpw; cb < ncols; cb += kWarps * gpw)
   {
-    df64* y = B + static_cast<int64_t>(q) * ldb;
+    const int q = cb + lane / G;
+    const bool act = q < ncols;
+    df64* y = B + static_cast<int64_t>(act ? q : cb) * ldb;
     df64 acc[kWyB];
 #pragma unroll
     for (int i = 0; i < kWyB; ++i)
       acc[i] = df64{0.0f, 0.0f};
-    for (int r = lane; r < hp; r += 32)
-    {
-      const df64 a = y[r];
+    if (act)
+      for (int r = gl; r < hp; r += G)
+      {
+        const df64 a = y[r];
 #pragma unroll
-      for (int i = 0; i < kWyB; ++i)
-        acc[i] = df_fma(P[r + static_cast<int64_t>(i) * hp], a, acc[i]);
-    }
+        for (int i = 0; i < kWyB; ++i)
+          acc[i] = df_fma(P[r + static_cast<int64_t>(i) * hp], a, acc[i]);
+      }
 #pragma unroll
     for (int i = 0; i < kWyB; ++i)
-      acc[i] = df_warp_sum(acc[i]);  // W = V^T y on every lane
-    // Lane li forms (T' W)_li, then every lane gathers all kWyB of them.
+      acc[i] = df_group_sum(acc[i], G);  // W = V^T y on every lane of the group
+    // Lane li of the group forms (T' W)_li; the group gathers all kWyB.
     df64 wp{0.0f, 0.0f};
 #pragma unroll
     for (int l = 0; l < kWyB; ++l)
       wp = df_fma(kTrans ? T[l + li * kWyB] : T[li + l * kWyB], acc[l], wp);
 #pragma unroll
     for (int i = 0; i < kWyB; ++i)
-      acc[i] = df_neg(df64{__shfl_sync(0xffffffffu, wp.hi, i), __shfl_sync(0xffffffffu, wp.lo, i)});
-    for (int r = lane; r < hp; r += 32)
-    {
-      df64 a = y[r];
+      acc[i] = df_neg(df64{__shfl_sync(0xffffffffu, wp.hi, gbase + i),
+                           __shfl_sync(0xffffffffu, wp.lo, gbase + i)});
+    if (act)
+      for (int r = gl; r < hp; r += G)
+      {
+        df64 a = y[r];
 #pragma unroll
-      for (int i = 0; i < kWyB; ++i)
-        a = df_fma(acc[i], P[r + static_cast<int64_t>(i) * hp], a);
-      y[r] = a;
-    }
+        for (int i = 0; i < kWyB; ++i)
+          a = df_fma(acc[i], P[r + static_cast<int64_t>(i) * hp], a);
+        y[r] = a;
+      }
   }
   __syncthreads();
 }
