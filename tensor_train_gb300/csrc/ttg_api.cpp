@@ -380,7 +380,7 @@ int64_t round_need(const Shape& s, int job_kind)
     if (k <= d - 2)
       cols += rp;
   }
-  need = std::max(need, a32(cols + 1));
+  need = std::max(need, a32(2 * (cols + 1)));  // balance: scale factors and inverses
   return need + 64;
 }
 

@@ -627,7 +627,7 @@ __device__ __noinline__ void balance(double* ar, CoreSlot* S, int d, Bump bump, 
   int64_t total = 0;
   for (int k = 0; k < d - 1; ++k)
     total += S[k].rp;
-  double* cn = bump.take(total + 1);
+  double* cn = bump.take(2 * (total + 1));  // norms -> scl, then 1 / scl
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   double my_log = 0.0, my_cnt = 0.0;
   int64_t base = 0;
@@ -659,31 +659,39 @@ __device__ __noinline__ void balance(double* ar, CoreSlot* S, int d, Bump bump, 
   if (tot_cnt <= 0.0)
     return;
   const double geo = exp(tot_log / tot_cnt);
+  // Per bond column: scl = geo / nc multiplies the column of left_unfold(c_k)
+  // and 1 / scl the matching row of right_unfold(c_{k+1}) (the reference
+  // divides by scl: the same up to the last bit), once per column here
+  // rather than per element.
+  double* inv = cn + total + 1;
+  for (int64_t t = threadIdx.x; t < total; t += blockDim.x)
+  {
+    const double nc = cn[t];
+    cn[t] = nc > 0.0 ? geo / nc : 1.0;
+    inv[t] = nc > 0.0 ? nc / geo : 1.0;
+  }
+  __syncthreads();
   base = 0;
   int64_t prev_base = 0;
   for (int k = 0; k < d; ++k)
   {
     const int r = S[k].r, n = S[k].n, c = S[k].rp;
     double* p = ar + S[k].off;
-    const int64_t sz = static_cast<int64_t>(r) * n * c;
-    for (int64_t t = threadIdx.x; t < sz; t += blockDim.x)
+    const int rows = r * n;
+    // cg lanes per row (a power of two >= c, at most 32), 32 / cg rows per
+    // warp at a time: no index division per element.
+    int cg = 1;
+    while (cg < c && cg < 32)
+      cg <<= 1;
+    const int rpw = 32 / cg, lb = lane & (cg - 1);
+    const double* fc = k <= d - 2 ? cn + base : nullptr;
+    const double* fr = k >= 1 ? inv + prev_base : nullptr;
+    for (int row = w * rpw + lane / cg; row < rows; row += kWarps * rpw)
     {
-      const int a = static_cast<int>(t / (static_cast<int64_t>(n) * c));
-      const int b = static_cast<int>(t % c);
-      double x = p[t];
-      if (k >= 1)
-      {
-        const double nr = cn[prev_base + a];
-        if (nr > 0.0)
-          x /= geo / nr;
-      }
-      if (k <= d - 2)
-      {
-        const double nc = cn[base + b];
-        if (nc > 0.0)
-          x *= geo / nc;
-      }
-      p[t] = x;
+      const double f = fr ? fr[row / n] : 1.0;
+      double* x = p + static_cast<int64_t>(row) * c;
+      for (int b = lb; b < c; b += cg)
+        x[b] *= fc ? f * fc[b] : f;
     }
     if (k <= d - 2)
     {
@@ -709,7 +717,7 @@ __device__ int64_t balance_need(const CoreSlot* S, int d)
   int64_t total = 0;
   for (int k = 0; k < d - 1; ++k)
     total += S[k].rp;
-  return a32(total + 1);
+  return a32(2 * (total + 1));
 }
 
 __device__ __noinline__ void round_tt(const RoundJob& job, int tti, double* scratch, Smem sm, CtaShared& sh,
@@ -976,7 +984,9 @@ __device__ __noinline__ void round_sketch_tt(const RoundJob& job, int tti, doubl
     double* tau = b2.take(l);
     double* Rq = b2.take(static_cast<int64_t>(l) * l);
     double* Q;
-    const int lq = qr_factor(View{Z, 1, h}, h, l, Wq, tau, Rq, Smem{nullptr, 0}, &Q, mixed, sh);
+    // The CTA's shared region is free here: the sketched QR stages in it
+    // (in place when h*l fits, else blocked with its panels staged there).
+    const int lq = qr_factor(View{Z, 1, h}, h, l, Wq, tau, Rq, sm, &Q, mixed, sh);
     // M (lq x rp) = Q^T left_unfold(cur).
     double* M = b2.take(static_cast<int64_t>(lq) * rp);
     gemm_sel(mixed, lq, rp, h, View{Q, h, 1}, View{ar + cur.off, rp, 1}, M, rp, 1, sh);

@@ -219,7 +219,7 @@ int64_t slab_need(const NoallocShape& s, bool right_canonical)
     if (k <= d - 2)
       cols += rp;
   }
-  need = imax64(need, a32(cols + 1));
+  need = imax64(need, a32(2 * (cols + 1)));  // balance: scale factors and inverses
   return need + 64;
 }
 

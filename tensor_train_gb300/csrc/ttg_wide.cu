@@ -588,7 +588,41 @@ __device__ bool wide_balance(const WideJob& job, double* ar, CoreSlot* S, int d,
   for (int k = 0; k < d; ++k)
   {
     const int r = S[k].r, n = S[k].n, c = S[k].rp;
-    if (k % P == me)
+    constexpr int kFactorCap = 16 * (64 + 1);  // doubles in each GEMM staging tile
+    if (k % P == me && r <= kFactorCap && c <= kFactorCap)
+    {
+      // This core's row and column factors, once each, in the CTA's GEMM
+      // staging tiles (free here): 1 / scl of bond k-1 per row block a,
+      // scl = geo / nc of bond k per column (the reference divides by scl:
+      // the same up to the last bit).
+      double* rf = &sh.gemm_a[0][0];
+      double* cf = &sh.gemm_b[0][0];
+      for (int a = threadIdx.x; a < r; a += blockDim.x)
+      {
+        const double nr = k >= 1 ? job.cn[prev_base + a] : 0.0;
+        rf[a] = nr > 0.0 ? nr / geo : 1.0;
+      }
+      for (int b = threadIdx.x; b < c; b += blockDim.x)
+      {
+        const double nc = k <= d - 2 ? job.cn[base + b] : 0.0;
+        cf[b] = nc > 0.0 ? geo / nc : 1.0;
+      }
+      __syncthreads();
+      int cg = 1;  // lanes per row: a power of two >= c, at most 32
+      while (cg < c && cg < 32)
+        cg <<= 1;
+      const int rpw = 32 / cg, lb = lane & (cg - 1);
+      double* p = ar + S[k].off;
+      for (int row = w * rpw + lane / cg; row < r * n; row += kWarps * rpw)
+      {
+        const double f = rf[row / n];
+        double* x = p + static_cast<int64_t>(row) * c;
+        for (int b = lb; b < c; b += cg)
+          x[b] *= f * cf[b];
+      }
+      __syncthreads();
+    }
+    else if (k % P == me)
     {
       double* p = ar + S[k].off;
       const int64_t sz = static_cast<int64_t>(r) * n * c;
