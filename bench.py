@@ -32,8 +32,9 @@ METRIC = ("TT roundings/sec and matvec_round/sec at rel. err<=1e-8: mixed/learne
 EPS = 1e-8
 SEED0 = 1000
 # DRAM bytes (read + write) of one mixed round_kernel launch on TTs 1000..1607
-# of the batch at 4 CTAs per SM (ncu, profiles/round_kernel_batch608_ncu.md).
-TRAFFIC_608 = 7.988859392e9 + 20.41651968e9
+# of the batch at the mixed default of 3 CTAs per SM (ncu,
+# profiles/round_kernel_batch608_ncu.md).
+TRAFFIC_608 = 6.161341952e9 + 9.316889088e9
 
 
 def measured_peaks(path=None):
@@ -344,8 +345,8 @@ def run_ours(args):
         "config": workload_config(count),
         "precision": "mixed", "parallelism": f"{world} independent shard(s), one GPU each",
         # traffic: DRAM read + write bytes of one mixed round_kernel launch at
-        # the benched 4 CTAs per SM, from the ncu capture of a 608-TT slice of
-        # this batch (7.989 GB read + 20.417 GB written), scaled to `count`
+        # the mixed default of 3 CTAs per SM, from the ncu capture of a 608-TT slice of
+        # this batch (6.161 GB read + 9.317 GB written), scaled to `count`
         # TTs by the TT count; it is per-CTA scratch of the work matrices
         # evicted from L2, set against the algorithmic bytes (input cores read,
         # output cores written).
