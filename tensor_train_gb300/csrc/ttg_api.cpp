@@ -11,6 +11,7 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <memory>
 #include <mutex>
 #include <numeric>
 #include <string>
@@ -1789,12 +1790,15 @@ static int32_t unpack_round(ttg_plan& P, const int32_t* orig, ttg_tensor* outs,
   });
 }
 
-// A large batch with host buffers runs as two plans whose host and device
-// phases overlap: chunk 1 is packed and uploaded while chunk 0 sweeps, and
-// chunk 0 is downloaded and unpacked while chunk 1 sweeps.  The chunks split
-// the batch by estimated sweep cost (largest first, each TT to the lighter
-// chunk) so that the two sweeps take about as long; each sweeps on its own
-// stream, so chunk 1's CTAs take the SMs that chunk 0's last TTs free.
+// A large batch with host buffers runs as a pipeline of plans whose host and
+// device phases overlap: chunk c + 1 is packed and uploaded while chunk c
+// sweeps, and chunk c is downloaded and unpacked while chunk c + 1 sweeps.
+// Two chunks are in flight at a time, each on its own stream with its own
+// pooled buffers (chunk c takes slot c % 2 once chunk c - 2 has been
+// unpacked); chunk c + 1's CTAs take the SMs that chunk c's last TTs free.
+// The chunks split the batch by estimated sweep cost (largest first, each TT
+// to the lightest chunk) so that the sweeps take about as long; the first
+// pack and the last unpack, a chunk each, are all that stays exposed.
 constexpr int32_t kPipelineMinBatch = 1024;
 
 static int32_t round_batch_pipelined(int32_t count, const ttg_tensor* ins,
@@ -1802,53 +1806,88 @@ static int32_t round_batch_pipelined(int32_t count, const ttg_tensor* ins,
                                      ttg_round_result* results, const char* op,
                                      const std::vector<double>& cost)
 {
+  const int nch = std::max(2, std::min(4, count / kPipelineMinBatch));
   std::vector<int32_t> order(static_cast<size_t>(count));
   std::iota(order.begin(), order.end(), 0);
   std::stable_sort(order.begin(), order.end(),
                    [&](int32_t a, int32_t b) { return cost[a] > cost[b]; });
-  std::vector<int32_t> part[2];
-  std::vector<ttg_tensor> cin[2];
-  double load[2] = {0.0, 0.0};
+  struct Chunk
+  {
+    std::vector<int32_t> part;
+    std::vector<ttg_tensor> in;
+    double load = 0.0;
+    ttg_plan P;
+    std::unique_ptr<PoolLease> lease;
+  };
+  std::vector<std::unique_ptr<Chunk>> ch;
+  for (int c = 0; c < nch; ++c)
+    ch.push_back(std::make_unique<Chunk>());
   for (int32_t i : order)
   {
-    const int c = load[0] <= load[1] ? 0 : 1;
-    part[c].push_back(i);
-    cin[c].push_back(ins[i]);
-    load[c] += cost[i];
+    int c = 0;
+    for (int j = 1; j < nch; ++j)
+      if (ch[j]->load < ch[c]->load)
+        c = j;
+    ch[c]->part.push_back(i);
+    ch[c]->in.push_back(ins[i]);
+    ch[c]->load += cost[i];
   }
   CallTrace trace;
-  ttg_plan P0, P1;
-  ttg_plan* P[2] = {&P0, &P1};
-  PoolLease lease0(P0, 0), lease1(P1, 1);
   const cudaStream_t st[2] = {lib_stream(), lib_stream2()};
-  for (int c = 0; c < 2; ++c)
-  {
-    if (int32_t e = build_round_plan(*P[c], static_cast<int32_t>(cin[c].size()), cin[c].data(),
-                                     opts, op))
+  auto launch = [&](int c) -> int32_t {
+    Chunk& k = *ch[c];
+    k.lease = std::make_unique<PoolLease>(k.P, c & 1);
+    if (int32_t e = build_round_plan(k.P, static_cast<int32_t>(k.in.size()), k.in.data(), opts, op))
       return e;
-    trace.mark(c ? "pack1" : "pack0");
-    if (int32_t e = plan_upload(*P[c], st[c]))
+    trace.mark("pack");
+    if (int32_t e = plan_upload(k.P, st[c & 1]))
       return e;
-    TTG_CUDA(cudaEventRecord(P[c]->ev0, st[c]));
-    if (int32_t e = plan_run(*P[c], st[c]))
+    TTG_CUDA(cudaEventRecord(k.P.ev0, st[c & 1]));
+    if (int32_t e = plan_run(k.P, st[c & 1]))
       return e;
-    TTG_CUDA(cudaEventRecord(P[c]->ev1, st[c]));
-  }
-  for (int c = 0; c < 2; ++c)
-  {
-    if (int32_t e = plan_download_raw(*P[c], st[c]))
+    TTG_CUDA(cudaEventRecord(k.P.ev1, st[c & 1]));
+    return TTG_OK;
+  };
+  auto finish = [&](int c) -> int32_t {
+    Chunk& k = *ch[c];
+    if (int32_t e = plan_download_raw(k.P, st[c & 1]))
       return e;
-    trace.mark(c ? "sweep1+d2h1" : "sweep0+d2h0");
+    trace.mark("sweep+d2h");
     float ms = 0.0f;
-    TTG_CUDA(cudaEventElapsedTime(&ms, P[c]->ev0, P[c]->ev1));
-    if (int32_t e = unpack_round(*P[c], part[c].data(), outs, results, ms))
+    TTG_CUDA(cudaEventElapsedTime(&ms, k.P.ev0, k.P.ev1));
+    if (int32_t e = unpack_round(k.P, k.part.data(), outs, results, ms))
       return e;
-    trace.mark(c ? "unpack1" : "unpack0");
+    trace.mark("unpack");
+    const int32_t bad = first_bad_status(k.P);
+    k.lease.reset();  // the slot's buffers back to the pool for chunk c + 2
+    if (bad)
+      return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
+    return TTG_OK;
+  };
+  auto run_all = [&]() -> int32_t {
+    for (int c = 0; c < std::min(nch, 2); ++c)
+      if (int32_t e = launch(c))
+        return e;
+    for (int c = 0; c < nch; ++c)
+    {
+      if (int32_t e = finish(c))
+        return e;
+      if (c + 2 < nch)
+        if (int32_t e = launch(c + 2))
+          return e;
+    }
+    return TTG_OK;
+  };
+  const int32_t e = run_all();
+  if (e)
+  {
+    // Nothing of a chunk still in flight may outlive its buffers' return
+    // to the pool.
+    cudaStreamSynchronize(st[0]);
+    cudaStreamSynchronize(st[1]);
+    return e;
   }
   trace.print(op, count);
-  for (int c = 0; c < 2; ++c)
-    if (int32_t bad = first_bad_status(*P[c]))
-      return fail(bad, std::string(op) + ": device status " + ttg_status_string(bad));
   return TTG_OK;
 }
 
