@@ -418,8 +418,9 @@ int32_t ttg_tc_gemm_f32(int32_t M, int32_t N, int32_t K, const float* A, int64_t
  * whose r*n, n*r' or r*n*r' alone exceeds the array.  The first call on each
  * device looks up the array's device address (cudaGetSymbolAddress) with
  * that device current, and so does the first call after a cudaDeviceReset
- * (the address is cached per device and context); make that first call
- * before any stream capture.  All calls share the array and it keeps the
+ * (the address is cached per device and context).  No call can be
+ * captured into a graph: each copies the ranks to the host and waits for
+ * its stream.  All calls share the array and it keeps the
  * last call's contents (every call resets what must start at zero); calls
  * that overlap on the GPU -- on different streams or threads -- race on it
  * and must be serialised by the caller.  The call waits for its own stream
