@@ -20,7 +20,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC"]
 SOURCES = ["ttg_kernels.cu", "ttg_wide.cu", "ttg_api.cpp", "ttg_host.cpp", "ttg_noalloc.cu",
            "ttg_mlp.cu", "ttg_tc_gemm.cu", "ttg_shard.cpp"]
 HEADERS = ["ttg_device.cuh", "ttg_device_df.cuh", "ttg_df64.cuh", "ttg_job.h", "ttg_kernels.h",
-           "ttg_tc.cuh", "ttg_sweep_common.cuh", "ttg_ozaki.cuh"]
+           "ttg_tc.cuh", "ttg_sweep_common.cuh", "ttg_ozaki.cuh", "ttg_wy_df.cuh", "ttg_gemm_live.h"]
 
 
 def _nvcc() -> str:

@@ -10,6 +10,8 @@
 #include <cstdint>
 #include <cuda_runtime.h>
 
+#include "ttg_gemm_live.h"
+
 namespace ttg
 {
 // Internal linkage: every translation unit that includes this header gets
@@ -397,22 +399,6 @@ enum GemmTri : int
   kTriUpperA = 1,
   kTriLowerB = 2,
 };
-
-// Rows (or columns) ty + 16 a, a < result, of a thread's 4 x 4 block that
-// lie inside the matrix (extent m from the tile start) and, for a
-// triangular factor, can be non-zero in the k slab [p0, p0 + 16) (index
-// <= p0 + 15 - tile start).
-__device__ __forceinline__ int gemm_live(int m_from_tile, int t, bool tri, int p0_from_tile)
-{
-  int n = (m_from_tile - t + 15) >> 4;
-  if (tri)
-  {
-    const int q = p0_from_tile + 15 - t;
-    const int nt = q < 0 ? 0 : (q >> 4) + 1;
-    n = nt < n ? nt : n;
-  }
-  return n < 0 ? 0 : (n > 4 ? 4 : n);
-}
 
 // One 64 x 64 tile of C = A B (FP64): k slabs of 16 staged in shared
 // memory, 4 x 4 outputs per thread.  A thread multiplies only the rows and
