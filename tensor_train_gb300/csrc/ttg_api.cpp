@@ -420,14 +420,14 @@ constexpr int kSmemOnePerSm = 25600;  // 200 KB
 constexpr int kSmemThreePerSm = 7168;  // 56 KB
 constexpr int kSmemFourPerSm = 4864;   // 38 KB
 
-// Whole-GPU schedule: chosen for round jobs (gauge none, method svd) by
+// Whole-GPU schedule: chosen for round jobs (method svd, both gauges) by
 // the options, or automatically for at most 4 TTs with a bond rank >= 64.
 // Work buffers are sized for the largest core and rank of the TTs swept.
 int32_t setup_wide(ttg_plan& P)
 {
   P.wide = false;
   const bool stream = P.job_kind == kJobStreamMatvec || P.job_kind == kJobStreamMatmat;
-  if ((P.job_kind != kJobRound && !stream) || P.order.empty() ||
+  if ((P.job_kind != kJobRound && P.job_kind != kJobRoundRight && !stream) || P.order.empty() ||
       P.opts.schedule == TTG_SCHED_PER_TT)
     return TTG_OK;
   // TTs whose cores the sweep touches: the rounded TTs, or every operand and

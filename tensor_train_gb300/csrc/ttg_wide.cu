@@ -938,6 +938,78 @@ __device__ bool wide_round_tt(const WideJob& job, int tti, WideSmem sm, CtaShare
   return true;
 }
 
+// round_right_canonical (round/tt_round.hpp:151-190) of TT tti over the
+// whole grid: the left-to-right QR sweep (left_qr_step,
+// detail/orthogonalize.hpp:35-60), the norm of the last core, then the
+// right-to-left truncated SVD sweep (svd_step_right, detail/truncate.hpp:
+// 114-166, a left step on the transposed unfolding), as round_tt of the
+// per-TT kernel does for kJobRoundRight.  No balancing.
+__device__ bool wide_round_right_tt(const WideJob& job, int tti, WideSmem sm, CtaShared& sh)
+{
+  TTInfo& T = job.tts[tti];
+  const int d = T.d;
+  CoreSlot* S = job.slots + T.first;
+  double* ar = job.arena;
+  const bool lead = (job.rank == 0 && threadIdx.x == 0);
+  if (d <= 1)
+    return true;
+  for (int k = 0; k < d - 1; ++k)
+  {
+    const int r = S[k].r, n = S[k].n, rp = S[k].rp;
+    const int h = r * n;
+    const int wn = S[k + 1].n * S[k + 1].rp;
+    double* cs = ar + S[k].off;
+    double* ns = ar + S[k + 1].off;
+    bool ok = true;
+    const int kk = wide_qr(job, View{cs, rp, 1}, h, rp, sm, sh, &ok);
+    if (!ok)
+      return false;
+    // core_k <- Q (h x kk, row-major); next (kk x wn) = R right_unfold(next),
+    // R (kk x rp) column-major in job.R.
+    wide_apply_q(job, h, kk, nullptr, 0, kk, cs, kk, 1, true, sm, sh);
+    if (!wide_gemm(job, kk, wn, rp, View{job.R, 1, kk}, View{ns, wn, 1}, job.Pb, wn, 1, sm, sh))
+      return false;
+    WSYNC();
+    wide_copy(job, ns, job.Pb, static_cast<int64_t>(kk) * wn);
+    if (lead)
+    {
+      set_ranks(S[k], r, kk);
+      set_ranks(S[k + 1], kk, S[k + 1].rp);
+    }
+    WSYNC();
+  }
+  double delta = 0.0;
+  const int st =
+    wide_norm_step(job, T, S, d, core_norm(ar + S[d - 1].off, core_size(S[d - 1]), sh), sh, &delta);
+  if (st != 0)
+    return st > 0;
+  for (int k = d - 1; k >= 1; --k)
+  {
+    const int r = S[k].r, n = S[k].n, rp = S[k].rp;
+    const int w = n * rp;
+    const int hp = S[k - 1].r * S[k - 1].n;
+    double* cs = ar + S[k].off;
+    double* ps = ar + S[k - 1].off;
+    int r_new = 1;
+    if (!wide_left_svd(job, View{cs, 1, w}, w, r, delta, T, nullptr, sm, sh, &r_new))
+      return false;
+    // prev (hp x r_new) = left_unfold(prev) F^T, F (r_new x r) row-major in
+    // job.F; core_k <- U^T, whose row-major layout is U's column-major one.
+    if (!wide_gemm(job, hp, r_new, r, View{ps, r, 1}, View{job.F, 1, r}, job.Pb, r_new, 1, sm, sh))
+      return false;
+    WSYNC();
+    wide_copy(job, ps, job.Pb, static_cast<int64_t>(hp) * r_new);
+    wide_copy(job, cs, job.Ub, static_cast<int64_t>(w) * r_new);
+    if (lead)
+    {
+      set_ranks(S[k], r_new, rp);
+      set_ranks(S[k - 1], S[k - 1].r, r_new);
+    }
+    WSYNC();
+  }
+  return true;
+}
+
 // Streaming apply-round (build_streaming_matvec / _matmat,
 // detail/streaming_apply.hpp:39-202, fused cores detail/fused_apply_core.hpp:
 // 33-272) over the whole grid: right-orthogonalise A and X, then per core
@@ -1122,8 +1194,10 @@ __global__ void __launch_bounds__(kThreads) wide_round_kernel(WideJob job)
     const bool stream = job.kind == kJobStreamMatvec || job.kind == kJobStreamMatmat;
     for (int i = team; i < job.ntt; i += teams)
     {
-      const bool ok = stream ? wide_stream_tt(tj, job.order ? job.order[i] : i, sm, sh)
-                             : wide_round_tt(tj, job.order ? job.order[i] : i, sm, sh);
+      const int item = job.order ? job.order[i] : i;
+      const bool ok = stream                        ? wide_stream_tt(tj, item, sm, sh)
+                      : job.kind == kJobRoundRight ? wide_round_right_tt(tj, item, sm, sh)
+                                                    : wide_round_tt(tj, item, sm, sh);
       if (!ok)
         break;
     }

@@ -221,3 +221,34 @@ def test_teams_schedule_batch(ttg, prec, tol):
     plan = ttg.Plan("round", ts, opts=_opts(ttg, 1e-8, ttg.schedule.teams))
     assert plan.schedule() == "teams"
     plan.close()
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_whole_gpu_round_right_canonical(ttg, prec):
+    # round_right_canonical over the whole grid (left-to-right QR sweep, then
+    # the right-to-left truncated SVD sweep): the oracle's ranks and tensor,
+    # right-orthogonal cores after the first; a keep-all and a truncating TT.
+    from tensor_train_gb300 import sketch
+    a = O.random([4] * 8, 32, 7, fan_in_scale=True)
+    b = O.random([4] * 8, 32, 8, fan_in_scale=True)
+    cores, _ = sketch.decaying_tt(5, d=12, n=4, terms=48, rho=0.6, rank8_every=8)
+    cases = [(O.add(a, b), 1e-8), ([np.ascontiguousarray(c) for c in cores], 1e-6)]
+    for t, eps in cases:
+        opts = _opts(ttg, eps, ttg.schedule.whole_gpu, gauge=ttg.round_gauge.right_canonical,
+                     precision=ttg.precision[prec])
+        info = ttg.RoundResult()
+        y = ttg.round(t, opts, info)
+        ref = O.round(t, eps, gauge="right_canonical")
+        if eps < 1e-7:
+            _close(y, ref, TOL if prec == "fp64" else 1e-10)
+        else:  # truncating: ranks within one of the oracle's, error within eps
+            assert max(abs(p - q) for p, q in zip(O.ranks(y), O.ranks(ref))) <= 1
+            assert O.rel_err(y, t) <= eps and O.rel_err(y, ref) <= 2 * eps
+        assert info.status == 0
+        for c in y[1:]:
+            m = c.reshape(c.shape[0], -1)
+            assert np.abs(m @ m.T - np.eye(m.shape[0])).max() <= 1e-10
+        per_tt = ttg.round(t, ttg.RoundOptions(eps=eps, gauge=ttg.round_gauge.right_canonical,
+                                               schedule=ttg.schedule.per_tt,
+                                               precision=ttg.precision[prec]))
+        assert O.ranks(per_tt) == O.ranks(y)
