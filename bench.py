@@ -54,14 +54,19 @@ def roofline_tensor(flops, kernel_ms, fp64_peak, traffic=None, **extra):
     """Roofline object of a rounding kernel against the dense BF16 tensor
     peak (the configured bound of the mixed path), with the FP64-pipe
     fraction beside it: the sweeps run no tensor-core work, so the tensor
-    fraction is small and the FP64 fraction is the informative one."""
+    fraction is small and the FP64 fraction is the informative one for the
+    plain FP64 kernel.  The mixed kernel does its arithmetic in df64 on the
+    FP32 pipes, so its algorithmic rate can exceed the FP64 peak."""
     _, bf16, src = measured_peaks()
     ach = flops / (kernel_ms / 1e3) / 1e12
     out = {"bound": "tensor", "achieved": ach, "peak": bf16, "unit": "TFLOP/s",
            "frac": ach / bf16, "traffic": traffic, "peak_source": src + ", dense BF16 burst",
            "fp64_pipe": {"achieved": ach, "peak": fp64_peak, "unit": "TFLOP/s",
                          "frac": ach / fp64_peak,
-                         "peak_source": "measured FP64 FMA loop on this GPU"},
+                         "peak_source": "measured FP64 FMA loop on this GPU",
+                         "note": "algorithmic FP64 flops over the FP64 FMA peak; a mixed-precision "
+                                 "kernel runs them as df64 on the FP32 pipes, so frac > 1 is "
+                                 "possible there"},
            "kernel_ms": kernel_ms, "flops_per_launch": flops}
     out.update(extra)
     return out
