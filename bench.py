@@ -87,6 +87,8 @@ def parse():
                     help="batch workload: time one precision only (profiling cases)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="keep the plan's default launch configuration (profiling cases)")
+    ap.add_argument("--gauge", choices=["none", "right_canonical"], default="none",
+                    help="round workloads: detail::round (none) or round_right_canonical")
     ap.add_argument("--workload", default="batch",
                     choices=["batch", "round_d10", "matvec_d20", "round_d40", "eval_d32",
                              "sketch_d64"],
@@ -519,8 +521,10 @@ def run_single(args):
     stream = torch.cuda.current_stream()
     sptr = stream.cuda_stream
     inp = single_inputs(T, args.workload, args.d, args.samples)
-    line = {"workload": args.workload, "metric": METRIC, "config": {"workload": inp["desc"]},
-            "steps": args.steps, "warmup": args.warmup, "precision": args.precision}
+    desc = inp["desc"] + (", gauge right_canonical" if args.gauge != "none" else "")
+    line = {"workload": args.workload, "metric": METRIC, "config": {"workload": desc},
+            "steps": args.steps, "warmup": args.warmup, "precision": args.precision,
+            "gauge": args.gauge}
 
     def timed(plan, tune=False):
         plan.upload(sptr)
@@ -615,7 +619,8 @@ def run_single(args):
     def measure(prec):
         opts = T.RoundOptions(eps=inp["eps"], precision=T.precision[prec],
                               schedule=T.schedule[args.schedule],
-                              method=T.round_method[args.method] if matvec else T.round_method.svd)
+                              method=T.round_method[args.method] if matvec else T.round_method.svd,
+                              gauge=T.round_gauge.none if matvec else T.round_gauge[args.gauge])
         plan = (T.Plan("matvec_round", inp["A"], inp["x"], opts=opts) if matvec
                 else T.Plan("round", [inp["tt"]], opts=opts))
         ms, clocks = timed(plan, tune=True)
@@ -668,7 +673,7 @@ def run_single(args):
         if matvec:
             ref = O.matvec_round(inp["A"], inp["x"], inp["eps"], method=args.method)
         else:
-            ref = O.round(inp["tt"], inp["eps"])
+            ref = O.round(inp["tt"], inp["eps"], gauge=args.gauge)
         sec = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": 1.0 / sec, "unit": unit, "cores": 1, "kind": "port",
                                 "sample": "one full call (oracle, 1 thread; a single TT does "
