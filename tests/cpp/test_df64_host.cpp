@@ -6,6 +6,10 @@
 //     (|lo| <= ulp(hi)/2), accuracy (2^-48 of |x 2^k| where lo is kept),
 //     round trips, signed zeros, infinities, NaN, the flush thresholds and
 //     the rounding carry out of the significand;
+//   * df_add / df_mul / df_fma against long double, within the double-word
+//     error bounds of Joldes, Muller & Popescu (ACM TOMS 2017: 3u^2 for
+//     DWPlusDW, 5u^2 for DWTimesDW with FMA; u = 2^-24), and the sum of
+//     the product's and the sum's bounds for the fused form;
 //   * df_recip and df_sqrt (one Newton step each) against long double;
 //   * gemm_live, the per-thread live-row rule of the GEMM tiles, against a
 //     brute-force enumeration of every product a tile must form.
@@ -110,6 +114,48 @@ static void check_split()
   CHECK(std::isinf(ttg::f32_to_f64_pow2(1.0f, 1100)), "f64 overflow");
 }
 
+static df64 random_pair(std::mt19937_64& rng)
+{
+  std::uniform_real_distribution<double> u(-1.0, 1.0);
+  std::uniform_int_distribution<int> ek(-20, 20);
+  return ttg::df_split_pow2(std::ldexp(u(rng), ek(rng)), 0);
+}
+
+static void check_ops()
+{
+  const long double u = 0x1p-24L;
+  std::mt19937_64 rng(5);
+  double wa = 0.0, wm = 0.0, wf = 0.0;
+  for (int it = 0; it < 300000; ++it)
+  {
+    const df64 a = random_pair(rng), b = random_pair(rng), c = random_pair(rng);
+    const long double av = pair_value(a), bv = pair_value(b), cv = pair_value(c);
+    const long double s = av + bv, p = av * bv, f = av * bv + cv;
+    if (s != 0.0L)
+    {
+      const long double e = std::fabs(pair_value(ttg::df_add(a, b)) - s) / std::fabs(s);
+      wa = std::fmax(wa, static_cast<double>(e / (u * u)));
+      CHECK(e <= 3 * u * u, "df_add err %Lg u^2", e / (u * u));
+    }
+    if (p != 0.0L)
+    {
+      const long double e = std::fabs(pair_value(ttg::df_mul(a, b)) - p) / std::fabs(p);
+      wm = std::fmax(wm, static_cast<double>(e / (u * u)));
+      CHECK(e <= 5 * u * u, "df_mul err %Lg u^2", e / (u * u));
+    }
+    // Fused: the product's error (relative to |ab|) plus the sum's (relative
+    // to the result), as an absolute bound.
+    const long double ef = std::fabs(pair_value(ttg::df_fma(a, b, c)) - f);
+    const long double bound = 5 * u * u * std::fabs(p) + 3 * u * u * (std::fabs(f) + std::fabs(p) * 5 * u * u);
+    if (f != 0.0L)
+      wf = std::fmax(wf, static_cast<double>(ef / (u * u * (std::fabs(p) + std::fabs(f)))));
+    CHECK(ef <= bound * (1 + 1e-6L) + 1e-300L, "df_fma err %Lg bound %Lg", ef, bound);
+  }
+  std::printf("ops: worst df_add %.2f u^2 (bound 3), df_mul %.2f u^2 (bound 5), df_fma %.2f u^2 of "
+              "|ab|+|ab+c|\n",
+              wa, wm, wf);
+}
+
 static void check_recip_sqrt()
 {
   std::mt19937_64 rng(11);
@@ -182,6 +228,7 @@ static void check_gemm_live()
 int main()
 {
   check_split();
+  check_ops();
   check_recip_sqrt();
   check_gemm_live();
   if (g_fail)
